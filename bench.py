@@ -1,0 +1,540 @@
+"""Benchmark of the GB300 path tracer (one JSON line on rank 0).
+
+Workloads
+  cornell   (default) Cornell box, 512 x 512, 16 spp, 8 bounces, NEE on,
+            Russian roulette off, seed 1. A step is one renderImage
+            (4,194,304 samples). Metric: Msamples/s.
+  traversal 1,000,000-triangle soup, 16,777,216 rays; a step is one
+            intersectClosest batch over all rays. Metric: Mrays/s.
+
+`value` is device time with inputs resident in HBM (CUDA events on the
+launching stream, max over ranks); `e2e` is the same metric through the
+C-ABI host-pointer call, host<->device copies included. Each rank renders
+its own samples (different frame indices / ray seeds): weak scaling, no
+data-path collective.
+
+--impl reference times the reference's CPU algorithm (the C++ restatement in
+oracle/, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+for _p in (ROOT / "caustic-tracer_gb300", ROOT / "tests"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import numpy as np  # noqa: E402
+
+CORNELL = dict(width=512, height=512, spp=16, max_bounces=8, russian_roulette=False, nee=True, seed=1)
+TRAVERSAL = dict(triangles=1_000_000, rays=16_777_216, scene_seed=2024, ray_seed=77)
+RAY_BYTES, HIT_BYTES, BOX_BYTES, TRI_BYTES, SPHERE_BYTES = 32, 16, 32, 48, 32
+ACCUM_BYTES_PER_SAMPLE = 12
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["cornell", "traversal"], default="cornell")
+    ap.add_argument("--small", action="store_true", help="reduced sizes for profiling captures")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ---- clocks ------------------------------------------------------------------------
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons every 200 ms while active."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ---- helpers -----------------------------------------------------------------------
+def peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        data = json.loads(path.read_text())
+        return float(data["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_record(workload: str):
+    path = ROOT / "profiles" / "traffic.json"
+    if path.exists():
+        return json.loads(path.read_text()).get(workload)
+    return None
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def max_over_ranks(x: float, world: int, device) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---- workloads --------------------------------------------------------------------
+def traversal_inputs(rank: int, small: bool):
+    import caustic as ct
+
+    tris = 100_000 if small else TRAVERSAL["triangles"]
+    nrays = 1 << 20 if small else TRAVERSAL["rays"]
+    packed = ct.pack_scene(ct.triangle_soup(tris, seed=TRAVERSAL["scene_seed"]))
+    rays = ct.soup_rays(nrays, seed=TRAVERSAL["ray_seed"] + rank)
+    return packed, rays
+
+
+def cornell_inputs(small: bool):
+    import caustic as ct
+
+    cfg = dict(CORNELL)
+    if small:
+        cfg.update(width=128, height=128, spp=4)
+    scene = ct.cornell_unit_box()
+    packed = ct.pack_scene(scene)
+    frame = ct.camera_frame(scene.camera, cfg["width"] / cfg["height"])
+    return packed, frame, cfg
+
+
+def cpu_reference(workload: str, small: bool, target_s: float = 12.0):
+    """Times the oracle (the reference algorithm in C++) on a bounded sample; returns a dict."""
+    import oracle_lib as oracle
+
+    threads = os.cpu_count() or 1
+    if workload == "traversal":
+        packed, rays = traversal_inputs(0, small)
+        n = 1 << 14
+        while True:
+            t0 = time.perf_counter()
+            _, _, _, _, cnt = oracle.trace(packed, rays[:n], 0, nthreads=threads)
+            dt = time.perf_counter() - t0
+            if dt >= target_s / 4 or n >= len(rays):
+                break
+            n = min(len(rays), int(n * max(2.0, min(8.0, target_s / 4 / max(dt, 1e-3)))))
+        bpr = RAY_BYTES + HIT_BYTES + (BOX_BYTES * cnt[0] + TRI_BYTES * cnt[1] + SPHERE_BYTES * cnt[2]) / n
+        return {"value": n / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                "sample": f"first {n} of the {len(rays)} rays, ordered walk (intersectClosest), {threads} threads",
+                "bytes_per_unit": bpr, "counts_per_ray": {"aabb": cnt[0] / n, "tri": cnt[1] / n, "sphere": cnt[2] / n},
+                "seconds": dt}
+    packed, frame, cfg = cornell_inputs(small)
+    from caustic import _abi
+
+    # Rows of the image at full spp until the sample takes long enough.
+    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
+    rows = 4
+    while True:
+        opts = _abi.ct_render_options(w, rows, spp, cfg["max_bounces"], int(cfg["russian_roulette"]),
+                                      int(cfg["nee"]), cfg["seed"])
+        fs = frame.struct()
+        t0 = time.perf_counter()
+        oracle.render_image(packed, fs, opts, nthreads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s / 4 or rows >= h:
+            break
+        rows = min(h, int(rows * max(2.0, min(8.0, target_s / 4 / max(dt, 1e-3)))))
+    samples = w * rows * spp
+    work = cornell_work_counts(packed, frame, cfg)
+    return {"value": samples / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"{w}x{rows} pixels x {spp} spp of the {w}x{h} render, {threads} threads",
+            "seconds": dt, "work_per_sample": work}
+
+
+def cornell_work_counts(packed, frame, cfg, npix: int = 8192):
+    """Mean work per sample of the reference algorithm (oracle) over a pixel subsample:
+    closest rays, shadow rays, and the box/triangle/sphere tests of each query kind."""
+    import oracle_lib as oracle
+    from caustic import _abi
+
+    topts = _abi.ct_trace_options(cfg["max_bounces"], int(cfg["russian_roulette"]), int(cfg["nee"]))
+    fs = frame.struct()
+    tot = np.zeros(10)
+    pixels = cfg["width"] * cfg["height"]
+    step = max(1, pixels // npix)
+    n = 0
+    for pixel in range(0, pixels, step):
+        _, work = oracle.pixel_radiance(packed, fs, cfg["width"], cfg["height"], pixel, cfg["seed"] * 7919, topts)
+        tot += work
+        n += 1
+    keys = ["closest_rays", "shadow_rays", "closest_aabb", "closest_tri", "closest_sphere", "closest_nodes",
+            "shadow_aabb", "shadow_tri", "shadow_sphere", "shadow_nodes"]
+    return {k: float(v) / n for k, v in zip(keys, tot)}
+
+
+def kernel_bytes_per_step(kernel: str, cpu: dict, units_per_step: int):
+    """Algorithmic bytes one step moves through `kernel`, from the reference's work counts.
+
+    Ray queries: 32 B per ray in, 16 B per closest hit out, 32 B per box test,
+    48 B per triangle test, 32 B per sphere test (the reference's ordered walk).
+    Shading: per closest-hit ray, 16 B hit + 32 B ray in, 48 B primitive +
+    64 B material read, 32 B continuation ray out, plus 44 B per shadow ray out.
+    Accumulation: 12 B read + 12 B written per sample.
+    """
+    if "bytes_per_unit" in cpu:  # traversal workload: one closest-hit query per unit
+        return cpu["bytes_per_unit"] * units_per_step if kernel == "trace" else None
+    w = cpu["work_per_sample"]
+    if kernel == "trace":
+        per = (w["closest_rays"] * (RAY_BYTES + HIT_BYTES) + w["shadow_rays"] * RAY_BYTES +
+               BOX_BYTES * (w["closest_aabb"] + w["shadow_aabb"]) + TRI_BYTES * (w["closest_tri"] + w["shadow_tri"]) +
+               SPHERE_BYTES * (w["closest_sphere"] + w["shadow_sphere"]))
+    elif kernel == "shade":
+        per = w["closest_rays"] * (16 + 32 + 48 + 64 + 32) + w["shadow_rays"] * 44
+    elif kernel == "accumulate":
+        per = 2 * ACCUM_BYTES_PER_SAMPLE
+    else:
+        return None
+    return per * units_per_step
+
+
+def run_reference(args, rank, world):
+    """The reference algorithm on the host cores: W warm-up and K timed steps, each step
+    one bounded sample of the workload (sized by a calibration run to ~2 s)."""
+    if rank != 0:
+        return
+    import oracle_lib as oracle
+    from caustic import _abi
+
+    threads = os.cpu_count() or 1
+    rec = cpu_reference(args.workload, args.small, target_s=8.0)
+    if args.workload == "traversal":
+        packed, rays = traversal_inputs(0, args.small)
+        n = max(1 << 12, min(len(rays), int(rec["value"] * 1e6 * 2.0)))
+        sample = rays[:n]
+        units = n
+
+        def step():
+            oracle.trace(packed, sample, 0, nthreads=threads)
+
+        desc = f"first {n} of the {len(rays)} rays per step, ordered walk (intersectClosest), {threads} threads"
+    else:
+        packed, frame, cfg = cornell_inputs(args.small)
+        w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
+        rows = max(1, min(h, int(rec["value"] * 1e6 * 2.0 / (w * spp))))
+        opts = _abi.ct_render_options(w, rows, spp, cfg["max_bounces"], int(cfg["russian_roulette"]),
+                                      int(cfg["nee"]), cfg["seed"])
+        fs = frame.struct()
+        units = w * rows * spp
+
+        def step():
+            oracle.render_image(packed, fs, opts, nthreads=threads)
+
+        desc = f"{w}x{rows} pixels x {spp} spp of the {w}x{h} render per step, {threads} threads"
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = units * args.steps / dt / 1e6
+    metric = "Msamples/s" if args.workload == "cornell" else "Mrays/s"
+    rec = {"value": value, "unit": metric, "cores": threads, "kind": "port", "sample": desc}
+    line = {
+        "impl": "reference", "metric": metric, "value": value, "unit": metric, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(args),
+        "cpu_baseline": {k: rec[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": rec["value"], "unit": metric, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    if args.workload == "traversal":
+        return {"workload": "traversal: 1,000,000-triangle soup, 16,777,216 rays, closest hit" if not args.small
+                else "traversal (small): 100,000 triangles, 1,048,576 rays",
+                "triangles": 100_000 if args.small else TRAVERSAL["triangles"],
+                "rays": (1 << 20) if args.small else TRAVERSAL["rays"],
+                "l2": "inputs larger than L2 (rays 512 MiB per step)", "parallelism": f"replicas x{args.gpus}"}
+    c = dict(CORNELL)
+    if args.small:
+        c.update(width=128, height=128, spp=4)
+    return {"workload": f"cornell box {c['width']}x{c['height']}, {c['spp']} spp, depth {c['max_bounces']}, NEE on, RR off",
+            **c, "l2": "L2 flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{args.gpus}"}
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import caustic as ct
+    from caustic import _abi, _native
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    device = torch.device("cuda", torch.cuda.current_device())
+    lib = _native.lib()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    hbm_peak, peak_kind = peaks()
+
+    if args.workload == "traversal":
+        packed, rays_np = traversal_inputs(rank, args.small)
+        n = len(rays_np)
+        dev = ct.DeviceScene(packed)
+        d_rays = torch.from_numpy(rays_np).to(device)
+        d_prim = torch.empty(n, dtype=torch.int32, device=device)
+        d_t = torch.empty(n, dtype=torch.float32, device=device)
+
+        def step():
+            _native.check(lib.ct_trace_closest_device(dev.handle, _native.ptr(d_rays), n, _native.ptr(d_prim),
+                                                      _native.ptr(d_t), None, None, C.c_void_p(stream.cuda_stream)))
+
+        units_per_step, metric, launches_per_step = n, "Mrays/s", 1
+    else:
+        packed, frame, cfg = cornell_inputs(args.small)
+        dev = ct.DeviceScene(packed)
+        w, h = cfg["width"], cfg["height"]
+        d_out = torch.empty(w * h * 3, dtype=torch.float32, device=device)
+        ropts = ct.RenderOptions(max_bounces=cfg["max_bounces"], russian_roulette=cfg["russian_roulette"],
+                                 nee=cfg["nee"], width=w, height=h, spp=cfg["spp"],
+                                 seed=cfg["seed"] + 104729 * rank).struct()
+        fs = frame.struct()
+
+        def step():
+            _native.check(lib.ct_render_image_device(dev.handle, C.byref(fs), C.byref(ropts), _native.ptr(d_out),
+                                                     C.c_void_p(stream.cuda_stream)))
+
+        units_per_step, metric = w * h * cfg["spp"], "Msamples/s"
+        launches_per_step = None
+
+    # warm-up
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.warmup)):
+            step()
+    torch.cuda.synchronize()
+    lib.ct_profile_reset() if hasattr(lib, "ct_profile_reset") else None
+    barrier(world)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        for k in range(args.steps):
+            if args.workload == "cornell":
+                flush.fill_(k & 0xFF)  # L2 flush outside the timed events
+            starts[k].record(stream)
+            step()
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = max_over_ranks(sum(step_ms) / 1e3, world, device)
+    value = units_per_step * args.steps * world / total_s / 1e6
+
+    prof = kernel_profile(lib, dev, step, stream, args)
+    if launches_per_step is None:
+        launches_per_step = prof.get("launches_per_step")
+
+    line = {
+        "metric": metric, "value": value, "unit": metric, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, Rng of the reference)",
+        "config": workload_config(args), "clocks": clocks.summary(), "gpu_launches": (launches_per_step or 0) * args.steps,
+    }
+
+    # CPU baseline (rank 0, N = 1): the oracle on a bounded sample; also yields the algorithmic bytes/unit.
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_reference(args.workload, args.small, target_s=12.0)
+        line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    line["roofline"] = roofline(args, prof, cpu, units_per_step, hbm_peak, peak_kind)
+
+    if not args.no_e2e:
+        line["e2e"] = e2e(args, ct, lib, packed, dev, rank, world, device)
+    dev.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def kernel_profile(lib, dev, step, stream, args):
+    """Per-kernel device times over a few profiled steps (CUDA events around every launch)."""
+    import torch
+
+    if not hasattr(lib, "ct_profile_enable"):
+        return {}
+    lib.ct_profile_enable(1)
+    lib.ct_profile_reset()
+    nsteps = max(2, min(args.steps, 5))
+    with torch.cuda.stream(stream):
+        for _ in range(nsteps):
+            step()
+    torch.cuda.synchronize()
+    names = (C.c_char_p * 32)()
+    ms = (C.c_double * 32)()
+    counts = (C.c_uint64 * 32)()
+    k = lib.ct_profile_read(names, ms, counts, 32)
+    lib.ct_profile_enable(0)
+    kernels = {names[i].decode(): {"ms": ms[i], "launches": int(counts[i])} for i in range(k)}
+    total_launches = sum(v["launches"] for v in kernels.values())
+    return {"kernels": kernels, "steps": nsteps, "launches_per_step": total_launches / nsteps}
+
+
+def roofline(args, prof, cpu, units_per_step, peak, peak_kind):
+    kernels = prof.get("kernels", {})
+    if not kernels:
+        return None
+    name, k = max(kernels.items(), key=lambda kv: kv[1]["ms"])
+    avg_ms = k["ms"] / k["launches"]
+    launches_per_step = k["launches"] / prof["steps"]
+    per_step = kernel_bytes_per_step(name, cpu, units_per_step) if cpu else None
+    algo = per_step / launches_per_step if per_step else None
+    rec = traffic_record(args.workload + ("_small" if args.small else ""))
+    achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_kind} hbm_gbs",
+            "traffic": rec.get("dram_bytes_per_launch") if rec else None,
+            "algorithmic_bytes_per_launch": algo, "avg_launch_ms": avg_ms,
+            "share": k["ms"] / sum(v["ms"] for v in kernels.values())}
+
+
+def e2e(args, ct, lib, packed, dev, rank, world, device):
+    """Same metric through the host-pointer C-ABI calls, copies included."""
+    import torch
+
+    from caustic import _abi, _native
+
+    steps = max(1, min(args.steps, 5))
+    if args.workload == "traversal":
+        _, rays_np = traversal_inputs(rank, args.small)
+        n = len(rays_np)
+        rays_pin = torch.from_numpy(rays_np).pin_memory()
+        prim_pin = torch.empty(n, dtype=torch.int32).pin_memory()
+        t_pin = torch.empty(n, dtype=torch.float32).pin_memory()
+        stats = _abi.ct_stats()
+
+        def call():
+            _native.check(lib.ct_trace_closest(dev.handle, C.c_void_p(rays_pin.data_ptr()), n,
+                                               C.c_void_p(prim_pin.data_ptr()), C.c_void_p(t_pin.data_ptr()),
+                                               None, None, C.byref(stats)))
+
+        h2d, d2h, units, metric = n * 32, n * 8, n, "Mrays/s"
+    else:
+        _, frame, cfg = cornell_inputs(args.small)
+        w, h = cfg["width"], cfg["height"]
+        out = torch.empty(w * h * 3, dtype=torch.float32).pin_memory()
+        ropts = ct.RenderOptions(max_bounces=cfg["max_bounces"], russian_roulette=cfg["russian_roulette"],
+                                 nee=cfg["nee"], width=w, height=h, spp=cfg["spp"],
+                                 seed=cfg["seed"] + 104729 * rank).struct()
+        fs = frame.struct()
+        view = packed.view()
+
+        def call():
+            handle = C.c_void_p()
+            _native.check(lib.ct_scene_create(C.byref(view), C.byref(handle)))
+            try:
+                _native.check(lib.ct_render_image(handle, C.byref(fs), C.byref(ropts),
+                                                  C.c_void_p(out.data_ptr()), None))
+            finally:
+                lib.ct_scene_destroy(handle)
+
+        h2d = packed.prims.nbytes + packed.nodes.nbytes + packed.mats.nbytes + packed.lights.nbytes + \
+            packed.prim_object.nbytes
+        d2h, units, metric = w * h * 12, w * h * cfg["spp"], "Msamples/s"
+    call()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        call()
+    dt = max_over_ranks(time.perf_counter() - t0, world, device)
+    return {"value": units * steps * world / dt / 1e6, "unit": metric, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "steps": steps}
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_gpu(args, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,288 @@
+// ct_scene_create / ct_scene_destroy: upload of a PackedScene (pack.ts:46-59).
+//
+// The host validates every index the kernels will follow (skip links, leaf
+// ranges, light and material indices) before anything reaches the device,
+// so a malformed array is rejected with CT_ERR_INVALID_ARGUMENT instead of
+// becoming an out-of-bounds read. It also derives the traversal layout the
+// kernels use: one 64-byte record per interior node holding both children's
+// boxes interleaved by axis plus the two child references, so a traversal
+// step is a single coalesced load instead of two dependent node loads.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "scene.hpp"
+
+namespace ct {
+
+ct_status DeviceBuffer::reserve(size_t want, size_t* total_bytes) {
+  if (want <= bytes) return CT_OK;
+  release(total_bytes);
+  size_t grow = want + want / 4;
+  cudaError_t err = cudaMalloc(&ptr, grow);
+  if (err != cudaSuccess) {
+    ptr = nullptr;
+    (void)cudaGetLastError();
+    err = cudaMalloc(&ptr, want);
+    grow = want;
+  }
+  if (err != cudaSuccess) {
+    ptr = nullptr;
+    (void)cudaGetLastError();
+    return fail(CT_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu bytes) failed: %s", want, cudaGetErrorString(err));
+  }
+  bytes = grow;
+  if (total_bytes) *total_bytes += grow;
+  return CT_OK;
+}
+
+void DeviceBuffer::release(size_t* total_bytes) {
+  if (ptr) {
+    cudaFree(ptr);
+    if (total_bytes) *total_bytes -= bytes;
+  }
+  ptr = nullptr;
+  bytes = 0;
+}
+
+namespace {
+
+bool is_index(float f, uint32_t limit) {
+  return f >= 0.0f && f < (float)limit && std::floor(f) == f;
+}
+
+// Structural check of the skip-link array (bvh.ts:319-381 invariants that the
+// traversals rely on) plus depth and the interior-record numbering.
+ct_status check_tree(const ct_packed_scene_view& v, std::vector<int32_t>& pair_of,
+                     uint32_t* interior_count, uint32_t* depth_out) {
+  const float* n = v.nodes;
+  const uint32_t N = v.node_count;
+  for (size_t i = 0; i < (size_t)N * CT_NODE_STRIDE; i++)
+    if (!std::isfinite(n[i])) return fail(CT_ERR_INVALID_ARGUMENT, "nodes[%zu] is not finite", i);
+  pair_of.assign(N, -1);
+  uint32_t interior = 0, depth = 0;
+  // Explicit post-order walk: frame = (node, depth, stage, end of left subtree).
+  struct F {
+    uint32_t node, depth, stage, after_left;
+  };
+  std::vector<F> st;
+  st.push_back({0, 1, 0, 0});
+  uint32_t ret = 0;
+  while (!st.empty()) {
+    F& f = st.back();
+    const float* r = n + (size_t)f.node * CT_NODE_STRIDE;
+    if (f.stage == 0) {
+      if (f.node >= N) return fail(CT_ERR_INVALID_ARGUMENT, "node index %u out of range", f.node);
+      if (f.depth > depth) depth = f.depth;
+      if (f.depth > N) return fail(CT_ERR_INVALID_ARGUMENT, "node links form a cycle");
+      if (r[7] >= 0.0f) {
+        if (!is_index(r[7], 1u << 24)) return fail(CT_ERR_INVALID_ARGUMENT, "node %u: bad leaf word", f.node);
+        const uint32_t word = (uint32_t)r[7], start = word >> 3, count = word & 7u;
+        if ((uint64_t)start + count > v.prim_count)
+          return fail(CT_ERR_INVALID_ARGUMENT, "node %u: leaf [%u, %u) beyond %u primitives", f.node, start,
+                      start + count, v.prim_count);
+        if (r[3] != (float)(f.node + 1)) return fail(CT_ERR_INVALID_ARGUMENT, "leaf %u: skip link is not %u", f.node, f.node + 1);
+        ret = f.node + 1;
+        st.pop_back();
+        continue;
+      }
+      pair_of[f.node] = (int32_t)interior++;
+      f.stage = 1;
+      const uint32_t child = f.node + 1, d = f.depth + 1;
+      st.push_back({child, d, 0, 0});
+      continue;
+    }
+    if (f.stage == 1) {
+      f.after_left = ret;
+      const float* left = n + (size_t)(f.node + 1) * CT_NODE_STRIDE;
+      if (left[3] != (float)ret) return fail(CT_ERR_INVALID_ARGUMENT, "node %u: skip link does not end its subtree", f.node + 1);
+      f.stage = 2;
+      const uint32_t child = ret, d = f.depth + 1;
+      st.push_back({child, d, 0, 0});
+      continue;
+    }
+    if (r[3] != (float)ret) return fail(CT_ERR_INVALID_ARGUMENT, "node %u: skip link does not end its subtree", f.node);
+    st.pop_back();
+  }
+  if (ret != N) return fail(CT_ERR_INVALID_ARGUMENT, "tree covers %u of %u nodes", ret, N);
+  *interior_count = interior;
+  *depth_out = depth;
+  return CT_OK;
+}
+
+int32_t child_ref(const float* n, const std::vector<int32_t>& pair_of, uint32_t child) {
+  const float* r = n + (size_t)child * CT_NODE_STRIDE;
+  if (r[7] >= 0.0f) return ~(int32_t)(uint32_t)r[7];
+  return pair_of[child];
+}
+
+ct_status validate_view(const ct_packed_scene_view& v) {
+  CT_CHECK_ARG(v.node_count == 0 || v.nodes != nullptr, "nodes is NULL");
+  CT_CHECK_ARG(v.prim_count == 0 || v.prims != nullptr, "prims is NULL");
+  CT_CHECK_ARG(v.prim_count == 0 || v.prim_object != nullptr, "prim_object is NULL");
+  CT_CHECK_ARG(v.light_count == 0 || v.lights != nullptr, "lights is NULL");
+  CT_CHECK_ARG(v.mats != nullptr || v.prim_count == 0, "mats is NULL");
+  CT_CHECK_ARG(v.prim_count < (1u << 21), "prim_count %u exceeds the float32 leaf encoding", v.prim_count);
+  CT_CHECK_ARG(v.node_count < (1u << 24), "node_count %u exceeds the float32 skip encoding", v.node_count);
+  const uint32_t mat_records = v.mat_count > 0 ? v.mat_count : 1;
+  for (uint32_t p = 0; p < v.prim_count; p++) {
+    const float* q = v.prims + (size_t)p * CT_PRIM_STRIDE;
+    for (int k = 0; k < CT_PRIM_STRIDE; k++)
+      if (!std::isfinite(q[k])) return fail(CT_ERR_INVALID_ARGUMENT, "prims[%u] has a non-finite value", p);
+    if (q[3] != CT_PRIM_SPHERE && q[3] != CT_PRIM_TRIANGLE)
+      return fail(CT_ERR_INVALID_ARGUMENT, "prims[%u]: unknown type %g", p, (double)q[3]);
+    if (v.prim_object[p] >= mat_records)
+      return fail(CT_ERR_INVALID_ARGUMENT, "prim_object[%u] = %u beyond %u materials", p, v.prim_object[p], mat_records);
+  }
+  for (uint32_t m = 0; m < v.mat_count; m++) {
+    const float* q = v.mats + (size_t)m * CT_MAT_STRIDE;
+    for (int k = 0; k < CT_MAT_STRIDE; k++)
+      if (!std::isfinite(q[k])) return fail(CT_ERR_INVALID_ARGUMENT, "mats[%u] has a non-finite value", m);
+    if (!(q[3] == 0 || q[3] == 1 || q[3] == 2 || q[3] == 3))
+      return fail(CT_ERR_INVALID_ARGUMENT, "mats[%u]: unknown type %g", m, (double)q[3]);
+  }
+  for (uint32_t l = 0; l < v.light_count; l++)
+    if (v.lights[l] < 0 || (uint32_t)v.lights[l] >= v.prim_count)
+      return fail(CT_ERR_INVALID_ARGUMENT, "lights[%u] = %d beyond %u primitives", l, v.lights[l], v.prim_count);
+  CT_CHECK_ARG(v.sky.kind == 0 || v.sky.kind == 1, "sky.kind %d is not 0 or 1", v.sky.kind);
+  return CT_OK;
+}
+
+template <class T>
+ct_status upload(ct_scene* s, DeviceBuffer& b, const T* src, size_t count, size_t min_count) {
+  const size_t n = count > min_count ? count : min_count;
+  ct_status st = b.reserve(n * sizeof(T), &s->device_bytes);
+  if (st != CT_OK) return st;
+  CT_CUDA(cudaMemsetAsync(b.ptr, 0, n * sizeof(T), s->stream));
+  if (count) CT_CUDA(cudaMemcpyAsync(b.ptr, src, count * sizeof(T), cudaMemcpyHostToDevice, s->stream));
+  return CT_OK;
+}
+
+void destroy(ct_scene* s) {
+  if (!s) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->pairs, &s->mats, &s->lights, &s->prim_object, &s->io,
+                          &s->counters, &s->paths.buf})
+    b->release(&s->device_bytes);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->ev2) cudaEventDestroy(s->ev2);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  cudaSetDevice(prev);
+  delete s;
+}
+
+ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
+  ct_status st = validate_view(v);
+  if (st != CT_OK) return st;
+  std::vector<int32_t> pair_of;
+  uint32_t interior = 0, depth = 0;
+  if (v.node_count > 0) {
+    st = check_tree(v, pair_of, &interior, &depth);
+    if (st != CT_OK) return st;
+  }
+  std::vector<float4> pairs((size_t)(interior > 0 ? interior : 1) * 4, make_float4(0, 0, 0, 0));
+  for (uint32_t i = 0; i < v.node_count; i++) {
+    const int32_t p = pair_of[i];
+    if (p < 0) continue;
+    const uint32_t left = i + 1, right = (uint32_t)v.nodes[(size_t)left * CT_NODE_STRIDE + 3];
+    const float* L = v.nodes + (size_t)left * CT_NODE_STRIDE;
+    const float* R = v.nodes + (size_t)right * CT_NODE_STRIDE;
+    float4* rec = &pairs[(size_t)p * 4];
+    rec[0] = make_float4(L[0], L[4], L[1], L[5]);
+    rec[1] = make_float4(R[0], R[4], R[1], R[5]);
+    rec[2] = make_float4(L[2], L[6], R[2], R[6]);
+    const int32_t cl = child_ref(v.nodes, pair_of, left), cr = child_ref(v.nodes, pair_of, right);
+    int32_t refs[4] = {cl, cr, 0, 0};
+    std::memcpy(&rec[3], refs, sizeof refs);
+  }
+
+  ct_scene* s = new (std::nothrow) ct_scene();
+  if (!s) return fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");
+  cudaGetDevice(&s->device);
+  auto bail = [&](ct_status code) {
+    destroy(s);
+    return code;
+  };
+  {
+    cudaError_t err = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (err != cudaSuccess) {
+      s->stream = nullptr;
+      return bail(fail(CT_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(err)));
+    }
+    if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess ||
+        cudaEventCreate(&s->ev2) != cudaSuccess)
+      return bail(fail(CT_ERR_CUDA, "cudaEventCreate failed"));
+  }
+  s->prim_count = v.prim_count;
+  s->node_count = v.node_count;
+  s->interior_count = interior;
+  s->mat_count = v.mat_count;
+  s->light_count = v.light_count;
+  s->depth = depth;
+  s->sky = v.sky;
+  if ((st = upload(s, s->prims, reinterpret_cast<const float4*>(v.prims), (size_t)v.prim_count * 4, 4)) != CT_OK ||
+      (st = upload(s, s->nodes, reinterpret_cast<const float4*>(v.nodes), (size_t)v.node_count * 2, 2)) != CT_OK ||
+      (st = upload(s, s->pairs, pairs.data(), pairs.size(), 4)) != CT_OK ||
+      (st = upload(s, s->mats, reinterpret_cast<const float4*>(v.mats), (size_t)v.mat_count * 4, 4)) != CT_OK ||
+      (st = upload(s, s->lights, v.lights, v.light_count, 1)) != CT_OK ||
+      (st = upload(s, s->prim_object, v.prim_object, v.prim_count, 1)) != CT_OK ||
+      (st = s->counters.reserve(kCounterWords * sizeof(uint32_t), &s->device_bytes)) != CT_OK)
+    return bail(st);
+  if (v.mat_count == 0 && v.mats != nullptr) {
+    // The reference always allocates one material record (pack.ts:122).
+    cudaError_t err = cudaMemcpyAsync(s->mats.ptr, v.mats, CT_MAT_STRIDE * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+    if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "material upload: %s", cudaGetErrorString(err)));
+  }
+  {
+    cudaError_t err = cudaMemsetAsync(s->counters.ptr, 0, kCounterWords * sizeof(uint32_t), s->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s->stream);
+    if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "scene upload: %s", cudaGetErrorString(err)));
+  }
+  ctk::SceneDev& d = s->dev;
+  d.prims = s->prims.as<float4>();
+  d.nodes = s->nodes.as<float4>();
+  d.pairs = s->pairs.as<float4>();
+  d.mats = s->mats.as<float4>();
+  d.lights = s->lights.as<int32_t>();
+  d.prim_object = s->prim_object.as<uint32_t>();
+  d.node_count = v.node_count;
+  d.light_count = v.light_count;
+  if (v.node_count > 0) {
+    d.root_ref = v.nodes[7] >= 0.0f ? ~(int32_t)(uint32_t)v.nodes[7] : pair_of[0];
+    for (int k = 0; k < 3; k++) {
+      d.root_lo[k] = v.nodes[k];
+      d.root_hi[k] = v.nodes[4 + k];
+    }
+  } else {
+    d.root_ref = ~0;  // an empty leaf; the kernels skip scenes without nodes
+  }
+  *out = s;
+  return CT_OK;
+}
+
+}  // namespace
+}  // namespace ct
+
+extern "C" {
+
+ct_status ct_scene_create(const ct_packed_scene_view* ps, ct_scene** out) {
+  ct::clear_error();
+  CT_CHECK_ARG(ps != nullptr && out != nullptr, "ct_scene_create: NULL argument");
+  *out = nullptr;
+  try {
+    return ct::create(*ps, out);
+  } catch (const std::bad_alloc&) {
+    return ct::fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");
+  }
+}
+
+void ct_scene_destroy(ct_scene* scene) { ct::destroy(scene); }
+
+uint64_t ct_scene_device_bytes(const ct_scene* scene) { return scene ? scene->device_bytes : 0; }
+
+}  // extern "C"

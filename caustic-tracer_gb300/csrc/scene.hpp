@@ -1,0 +1,68 @@
+// Device-resident scene of libcaustic_gb300 (the object behind ct_scene*).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+
+#include "common.hpp"
+#include "traverse.cuh"
+
+namespace ct {
+
+#define CT_CUDA(call)                                                                 \
+  do {                                                                                \
+    cudaError_t err_ = (call);                                                        \
+    if (err_ != cudaSuccess)                                                          \
+      return ::ct::fail(err_ == cudaErrorMemoryAllocation ? CT_ERR_OUT_OF_MEMORY      \
+                                                          : CT_ERR_CUDA,              \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(err_), __FILE__, __LINE__); \
+  } while (0)
+
+// Growable device allocation owned by a scene.
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  ct_status reserve(size_t want, size_t* total_bytes);
+  void release(size_t* total_bytes);
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(ptr);
+  }
+};
+
+// Per-scene wavefront state of the integrator (see integrator.cu).
+struct PathState {
+  DeviceBuffer buf;          // all per-path arrays, carved from one allocation
+  uint64_t capacity = 0;     // paths the buffer holds
+};
+
+}  // namespace ct
+
+struct ct_scene {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex lock;
+
+  // Device copies of the packed arrays plus the interior pair records.
+  ct::DeviceBuffer prims, nodes, pairs, mats, lights, prim_object;
+  uint32_t prim_count = 0, node_count = 0, interior_count = 0, mat_count = 0, light_count = 0;
+  uint32_t depth = 0;  // deepest root-to-leaf path, in nodes
+  ct_sky sky{};
+  ctk::SceneDev dev{};
+
+  // Staging for host-pointer entry points and per-call counters.
+  ct::DeviceBuffer io;
+  ct::DeviceBuffer counters;  // uint32 fp64-fallback counter and error flag
+  ct::PathState paths;
+  size_t device_bytes = 0;
+
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+};
+
+namespace ct {
+// Counters block layout (uint32 words).
+enum CounterWord : int { kCountFallbacks = 0, kCountError = 1, kCountQueue = 2, kCounterWords = 64 };
+}  // namespace ct

@@ -1,0 +1,187 @@
+// Batched ray queries: intersectClosest (intersect.ts:202-282) and occluded
+// (intersect.ts:368-420) over device-resident scenes.
+//
+// One thread per ray in a grid-stride loop sized to the resident capacity of
+// the 152 SMs. A ray is two float4 loads (32 B); results are written with
+// coalesced 4-byte stores.
+#include <atomic>
+#include <cstring>
+
+#include "scene.hpp"
+
+namespace ct {
+
+namespace {
+
+std::atomic<int32_t> g_variant{0};  // 0 ordered short-stack walk, 1 stackless skip links
+
+template <int VARIANT, bool ANY>
+__global__ void __launch_bounds__(128) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
+                                               uint32_t n, int32_t* __restrict__ prim,
+                                               float* __restrict__ t_out, float* __restrict__ u_out,
+                                               float* __restrict__ v_out,
+                                               uint8_t* __restrict__ blocked,
+                                               uint32_t* __restrict__ counters) {
+  uint32_t fallbacks = 0;
+  bool overflow = false;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float4 r0 = __ldg(rays + 2 * (size_t)i), r1 = __ldg(rays + 2 * (size_t)i + 1);
+    ctk::RayF r{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, 0.0f, 0.0f, 0.0f};
+    ctk::finish_ray(r);
+    ctk::HitF h{-1, r.tmax, 0.0f, 0.0f};
+    if (s.node_count > 0) {
+      if (VARIANT == 0)
+        overflow |= !ctk::walk_ordered<ANY>(s, r, h, fallbacks);
+      else
+        ctk::walk_stackless<ANY>(s, r, h, fallbacks);
+    }
+    if (ANY) {
+      blocked[i] = h.prim >= 0 ? 1 : 0;
+    } else {
+      prim[i] = h.prim;
+      t_out[i] = h.prim >= 0 ? h.t : INFINITY;
+      if (u_out) u_out[i] = h.prim >= 0 ? h.u : 0.0f;
+      if (v_out) v_out[i] = h.prim >= 0 ? h.v : 0.0f;
+    }
+  }
+  if (fallbacks) atomicAdd(&counters[kCountFallbacks], fallbacks);
+  if (overflow) atomicOr(&counters[kCountError], 1u);
+}
+
+template <int VARIANT, bool ANY>
+int grid_for(uint32_t n) {
+  static int per_sm = -1, sms = 0;
+  if (per_sm < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<VARIANT, ANY>, 128, 0);
+    if (per_sm < 1) per_sm = 1;
+  }
+  const uint64_t need = ((uint64_t)n + 127) / 128;
+  const uint64_t full = (uint64_t)sms * (uint64_t)per_sm;
+  return (int)(need < full ? (need > 0 ? need : 1) : full);
+}
+
+template <bool ANY>
+ct_status launch(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, float* t, float* u,
+                 float* v, uint8_t* blocked, cudaStream_t stream) {
+  if (n == 0) return CT_OK;
+  // A tree deeper than the ordered walk's stack uses the stackless walk.
+  const int variant = (g_variant.load() == 1 || s->depth > ctk::kStackSize) ? 1 : 0;
+  const float4* r4 = reinterpret_cast<const float4*>(rays);
+  uint32_t* cnt = s->counters.as<uint32_t>();
+  if (variant == 0)
+    k_trace<0, ANY><<<grid_for<0, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+  else
+    k_trace<1, ANY><<<grid_for<1, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+  CT_CUDA(cudaGetLastError());
+  return CT_OK;
+}
+
+// Host-pointer query: stage the rays, run, copy the results back.
+template <bool ANY>
+ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, float* t, float* u,
+                     float* v, uint8_t* blocked, ct_stats* stats) {
+  CT_CHECK_ARG(s != nullptr, "scene is NULL");
+  CT_CHECK_ARG(n == 0 || rays != nullptr, "rays is NULL");
+  CT_CHECK_ARG(n == 0 || (ANY ? blocked != nullptr : (prim != nullptr && t != nullptr)), "output is NULL");
+  std::lock_guard<std::mutex> guard(s->lock);
+  CT_CUDA(cudaSetDevice(s->device));
+  if (stats) std::memset(stats, 0, sizeof *stats);
+  if (n == 0) return CT_OK;
+  const size_t ray_bytes = (size_t)n * CT_RAY_FLOATS * sizeof(float);
+  const size_t out_words = ANY ? ((size_t)n + 3) / 4 : (size_t)n * (2 + (u ? 1 : 0) + (v ? 1 : 0));
+  ct_status st = s->io.reserve(ray_bytes + out_words * 4, &s->device_bytes);
+  if (st != CT_OK) return st;
+  char* base = s->io.as<char>();
+  float* d_rays = reinterpret_cast<float*>(base);
+  char* o = base + ray_bytes;
+  int32_t* d_prim = nullptr;
+  float *d_t = nullptr, *d_u = nullptr, *d_v = nullptr;
+  uint8_t* d_blocked = nullptr;
+  if (ANY) {
+    d_blocked = reinterpret_cast<uint8_t*>(o);
+  } else {
+    d_prim = reinterpret_cast<int32_t*>(o);
+    d_t = reinterpret_cast<float*>(o) + n;
+    size_t next = 2;
+    if (u) d_u = reinterpret_cast<float*>(o) + (next++) * (size_t)n;
+    if (v) d_v = reinterpret_cast<float*>(o) + (next++) * (size_t)n;
+  }
+  cudaStream_t stream = s->stream;
+  CT_CUDA(cudaMemsetAsync(s->counters.ptr, 0, 2 * sizeof(uint32_t), stream));
+  CT_CUDA(cudaEventRecord(s->ev0, stream));
+  CT_CUDA(cudaMemcpyAsync(d_rays, rays, ray_bytes, cudaMemcpyHostToDevice, stream));
+  CT_CUDA(cudaEventRecord(s->ev1, stream));
+  st = launch<ANY>(s, d_rays, n, d_prim, d_t, d_u, d_v, d_blocked, stream);
+  if (st != CT_OK) return st;
+  CT_CUDA(cudaEventRecord(s->ev2, stream));
+  if (ANY) {
+    CT_CUDA(cudaMemcpyAsync(blocked, d_blocked, n, cudaMemcpyDeviceToHost, stream));
+  } else {
+    CT_CUDA(cudaMemcpyAsync(prim, d_prim, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+    CT_CUDA(cudaMemcpyAsync(t, d_t, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+    if (u) CT_CUDA(cudaMemcpyAsync(u, d_u, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+    if (v) CT_CUDA(cudaMemcpyAsync(v, d_v, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+  }
+  uint32_t counters[2] = {0, 0};
+  CT_CUDA(cudaMemcpyAsync(counters, s->counters.ptr, sizeof counters, cudaMemcpyDeviceToHost, stream));
+  CT_CUDA(cudaStreamSynchronize(stream));
+  if (counters[1]) return fail(CT_ERR_UNSUPPORTED, "traversal stack overflow (tree depth %u)", s->depth);
+  if (stats) {
+    float k_ms = 0, all_ms = 0;
+    cudaEventElapsedTime(&k_ms, s->ev1, s->ev2);
+    cudaEventElapsedTime(&all_ms, s->ev0, s->ev2);
+    stats->kernel_ms = k_ms;
+    stats->total_ms = all_ms;
+    stats->rays = n;
+    stats->fp64_fallbacks = counters[0];
+    stats->launches = 1;
+  }
+  return CT_OK;
+}
+
+}  // namespace
+}  // namespace ct
+
+extern "C" {
+
+int32_t ct_set_traversal(int32_t variant) {
+  return ct::g_variant.exchange(variant == 1 ? 1 : 0);
+}
+
+ct_status ct_trace_closest(ct_scene* scene, const float* rays, uint32_t count, int32_t* prim,
+                           float* t, float* u, float* v, ct_stats* stats) {
+  ct::clear_error();
+  return ct::host_query<false>(scene, rays, count, prim, t, u, v, nullptr, stats);
+}
+
+ct_status ct_trace_occluded(ct_scene* scene, const float* rays, uint32_t count, uint8_t* blocked,
+                            ct_stats* stats) {
+  ct::clear_error();
+  return ct::host_query<true>(scene, rays, count, nullptr, nullptr, nullptr, nullptr, blocked, stats);
+}
+
+ct_status ct_trace_closest_device(ct_scene* scene, const float* rays, uint32_t count,
+                                  int32_t* prim, float* t, float* u, float* v, void* stream) {
+  ct::clear_error();
+  CT_CHECK_ARG(scene != nullptr, "scene is NULL");
+  CT_CHECK_ARG(count == 0 || (rays && prim && t), "NULL device pointer");
+  CT_CUDA(cudaSetDevice(scene->device));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : scene->stream;
+  return ct::launch<false>(scene, rays, count, prim, t, u, v, nullptr, s);
+}
+
+ct_status ct_trace_occluded_device(ct_scene* scene, const float* rays, uint32_t count,
+                                   uint8_t* blocked, void* stream) {
+  ct::clear_error();
+  CT_CHECK_ARG(scene != nullptr, "scene is NULL");
+  CT_CHECK_ARG(count == 0 || (rays && blocked), "NULL device pointer");
+  CT_CUDA(cudaSetDevice(scene->device));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : scene->stream;
+  return ct::launch<true>(scene, rays, count, nullptr, nullptr, nullptr, nullptr, blocked, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+"""GPU ray queries (ct_trace_closest / ct_trace_occluded) against the oracle.
+
+Parity bar: the hit primitive index equals the reference's (the oracle's
+float64 ordered walk) bit for bit, except at ties, where the GPU's primitive
+must itself be hit (in float64) at a distance within 1e-5 relative of the
+reference's closest t. Misses and occlusion flags must match exactly.
+"""
+import numpy as np
+import pytest
+
+import caustic as ct
+from test_oracle_bvh import closest_rays_99, finite_tmax_rays
+
+pytestmark = pytest.mark.gpu
+TIE_REL = 1e-5
+
+
+def check_closest(oracle, packed, rays, hits, label=""):
+    p, t, u, v, _ = oracle.trace(packed, rays, 0)
+    assert np.array_equal(p < 0, hits.prim < 0), f"{label}: hit/miss differs"
+    diff = np.nonzero(p != hits.prim)[0]
+    for i in diff:
+        t_gpu_prim = oracle.prim_hit_t(packed, int(hits.prim[i]), rays[i])
+        assert t_gpu_prim > 0, f"{label}: ray {i}: GPU prim {hits.prim[i]} is not hit in float64"
+        assert abs(t_gpu_prim - t[i]) <= TIE_REL * t[i], f"{label}: ray {i}: not a tie ({t_gpu_prim} vs {t[i]})"
+    hit = p >= 0
+    if hit.any():
+        rel = np.abs(hits.t[hit].astype(np.float64) - t[hit]) / t[hit]
+        assert rel.max() <= 4e-6, f"{label}: t relative error {rel.max()}"
+    assert np.isinf(hits.t[~hit]).all()
+    return len(diff), int(hit.sum())
+
+
+@pytest.fixture(scope="module")
+def random_scene(native_lib):
+    packed = ct.pack_scene(ct.random_test_scene(ct.Rng(1234), 1000, 2000))
+    with ct.DeviceScene(packed) as dev:
+        yield packed, dev
+
+
+@pytest.mark.parametrize("variant", ["ordered", "stackless"])
+def test_closest_matches_reference_rays(oracle, random_scene, variant):  # bvh.test.ts:88-112
+    packed, dev = random_scene
+    prev = ct.set_traversal(variant)
+    try:
+        rays = closest_rays_99()
+        hits = ct.intersect_closest(dev, rays, barycentrics=True)
+        ties, n_hit = check_closest(oracle, packed, rays, hits, variant)
+        assert n_hit > 500 and ties == 0
+        p, t, u, v, _ = oracle.trace(packed, rays, 0)
+        tri = (p >= 0) & (packed.prims[p.clip(0) * 16 + 3] == 1)
+        assert np.abs(hits.u[tri] - u[tri]).max() < 1e-5
+        assert np.abs(hits.v[tri] - v[tri]).max() < 1e-5
+    finally:
+        ct.set_traversal(prev)
+
+
+@pytest.mark.parametrize("variant", ["ordered", "stackless"])
+def test_closest_many_rays_and_finite_tmax(oracle, random_scene, variant):  # bvh.test.ts:114-131
+    packed, dev = random_scene
+    prev = ct.set_traversal(variant)
+    try:
+        r = ct.Rng(2024)
+        n = 200_000
+        u = r.draw(n * 6).reshape(n, 6)
+        o = -14 + 28 * u[:, :3]
+        d = (-8 + 16 * u[:, 3:]) - o
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        rays = ct.make_rays(o, d)
+        hits = ct.intersect_closest(dev, rays)
+        check_closest(oracle, packed, rays, hits, "200k")
+        rays = finite_tmax_rays(5, 300, 0.5, 20)
+        hits = ct.intersect_closest(dev, rays)
+        check_closest(oracle, packed, rays, hits, "tmax")
+        assert (hits.t[hits.prim >= 0] < rays[hits.prim >= 0, 7]).all()
+    finally:
+        ct.set_traversal(prev)
+
+
+@pytest.mark.parametrize("variant", ["ordered", "stackless"])
+def test_occluded_matches_reference(oracle, random_scene, variant):  # bvh.test.ts:134-146
+    packed, dev = random_scene
+    prev = ct.set_traversal(variant)
+    try:
+        rays = finite_tmax_rays(7, 500, 1, 30)
+        assert np.array_equal(ct.occluded(dev, rays), oracle.occluded(packed, rays)[0])
+        rays = finite_tmax_rays(8, 100_000, 0.01, 30, span=14)
+        assert np.array_equal(ct.occluded(dev, rays), oracle.occluded(packed, rays)[0])
+    finally:
+        ct.set_traversal(prev)
+
+
+def test_triangle_soup_parity(oracle, native_lib):
+    packed = ct.pack_scene(ct.triangle_soup(100_000, seed=5))
+    rays = ct.soup_rays(500_000, seed=6)
+    with ct.DeviceScene(packed) as dev:
+        hits = ct.intersect_closest(dev, rays)
+        ties, n_hit = check_closest(oracle, packed, rays, hits, "soup")
+        assert n_hit > 0.5 * len(rays)
+        assert ties <= 50
+
+
+def test_degenerate_scenes(oracle, native_lib):  # bvh.test.ts:148-169
+    from caustic.scene import Lambertian, Scene, SceneObject, Sphere
+
+    cam = ct.CORNELL_BOX.camera
+    empty = ct.pack_scene(Scene("empty", [], cam))
+    with ct.DeviceScene(empty) as dev:
+        hits = ct.intersect_closest(dev, np.array([[0, 0, 0, 0, 0, 1, 1e-4, np.inf]], np.float32))
+        assert hits.prim[0] == -1 and np.isinf(hits.t[0])
+    same = [SceneObject(f"c{i}", "c", Sphere((1, 2, 3), 0.5), Lambertian((1, 1, 1))) for i in range(40)]
+    co = ct.pack_scene(Scene("c", same, cam))
+    with ct.DeviceScene(co) as dev:
+        hits = ct.intersect_closest(dev, np.array([[1, 2, -5, 0, 0, 1, 1e-4, np.inf]], np.float32))
+        assert hits.prim[0] >= 0 and abs(hits.t[0] - 7.5) < 1e-5
+    one = ct.pack_scene(Scene("one", same[:1], cam))  # the root is a leaf
+    with ct.DeviceScene(one) as dev:
+        hits = ct.intersect_closest(dev, np.array([[1, 2, -5, 0, 0, 1, 1e-4, np.inf],
+                                                   [1, 2, 3, 0, 0, 1, 1e-4, np.inf],
+                                                   [9, 9, 9, 0, 0, 1, 1e-4, np.inf]], np.float32))
+        assert list(hits.prim) == [0, 0, -1]
+        assert abs(hits.t[0] - 7.5) < 1e-5 and abs(hits.t[1] - 0.5) < 1e-6
+
+
+def test_ragged_batch_sizes(oracle, random_scene):
+    packed, dev = random_scene
+    rays_all = closest_rays_99(1000)
+    for n in (0, 1, 31, 32, 33, 127, 128, 129, 999):
+        hits = ct.intersect_closest(dev, rays_all[:n])
+        assert len(hits.prim) == n
+        if n:
+            check_closest(oracle, packed, rays_all[:n], hits, f"n={n}")
