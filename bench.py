@@ -51,6 +51,7 @@ def parse_args():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["cornell", "traversal"], default="cornell")
     ap.add_argument("--small", action="store_true", help="reduced sizes for profiling captures")
+    ap.add_argument("--rays", type=int, default=0, help="traversal: trace only this many rays (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -150,11 +151,11 @@ def barrier(world: int):
 
 
 # ---- workloads --------------------------------------------------------------------
-def traversal_inputs(rank: int, small: bool):
+def traversal_inputs(rank: int, small: bool, rays: int = 0):
     import caustic as ct
 
     tris = 100_000 if small else TRAVERSAL["triangles"]
-    nrays = 1 << 20 if small else TRAVERSAL["rays"]
+    nrays = rays or ((1 << 20) if small else TRAVERSAL["rays"])
     packed = ct.pack_scene(ct.triangle_soup(tris, seed=TRAVERSAL["scene_seed"]))
     rays = ct.soup_rays(nrays, seed=TRAVERSAL["ray_seed"] + rank)
     return packed, rays
@@ -246,7 +247,7 @@ def kernel_bytes_per_step(kernel: str, cpu: dict, units_per_step: int):
     Accumulation: 12 B read + 12 B written per sample.
     """
     if "bytes_per_unit" in cpu:  # traversal workload: one closest-hit query per unit
-        return cpu["bytes_per_unit"] * units_per_step if kernel == "trace" else None
+        return cpu["bytes_per_unit"] * units_per_step if kernel == "closest" else None
     w = cpu["work_per_sample"]
     if kernel == "trace":
         per = (w["closest_rays"] * (RAY_BYTES + HIT_BYTES) + w["shadow_rays"] * RAY_BYTES +
@@ -342,7 +343,7 @@ def run_gpu(args, rank, world):
     hbm_peak, peak_kind = peaks()
 
     if args.workload == "traversal":
-        packed, rays_np = traversal_inputs(rank, args.small)
+        packed, rays_np = traversal_inputs(rank, args.small, args.rays)
         n = len(rays_np)
         dev = ct.DeviceScene(packed)
         d_rays = torch.from_numpy(rays_np).to(device)

@@ -25,6 +25,7 @@
 #include "profile.hpp"
 #include "scene.hpp"
 
+
 namespace ct {
 
 namespace {
@@ -32,6 +33,7 @@ namespace {
 constexpr int kBlock = 128;
 constexpr int kWarps = kBlock / 32;
 constexpr uint64_t kMaxWavePaths = 8ull << 20;  // paths in flight per wave
+constexpr uint32_t kPersistentDepth = 16;      // tree depth above which traces refill lanes
 
 // Path state of one queue slot (3 x 16 bytes, read and written coalesced):
 //   a = origin.xyz, rng state      b = dir.xyz, pdf (< 0: last bounce specular)
@@ -57,7 +59,7 @@ struct WaveArgs {
   int32_t* hit_prim;
   float* hit_t;
   float4* radiance;      // per path id: accumulated L (w unused)
-  uint32_t* counts;      // [0, B+2): path queue sizes; [B+2, 2B+4): shadow queue sizes
+  uint32_t* counts;      // queue sizes and counters, layout in run_passes
   uint32_t width, height, pixels, paths, first_frame;
   int32_t max_bounces, rr, nee;
   float sky_zenith[3], sky_horizon[3], sky_strength;
@@ -116,37 +118,52 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
 }
 
 // Closest hits of the bounce-b path queue plus the shadow rays of bounce b-1.
-__global__ void __launch_bounds__(kBlock) k_trace(WaveArgs a, int32_t bounce) {
+// PERSISTENT: lanes refill from a work counter as their walks finish (pays
+// off for deep trees); otherwise one walk per thread in a grid-stride loop
+// (cheaper for shallow trees, where walks are short and even).
+template <bool PERSISTENT>
+__global__ void __launch_bounds__(kBlock, 8) k_trace(WaveArgs a, int32_t bounce) {
   const uint32_t n_ext = bounce <= a.max_bounces ? a.counts[bounce] : 0u;
   const uint32_t n_sh = bounce > 0 ? a.counts[a.max_bounces + 2 + bounce - 1] : 0u;
-  const uint32_t total = n_ext + n_sh;
-  const uint32_t stride = gridDim.x * blockDim.x;
   uint32_t fallbacks = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+  // Query i < n_ext: closest hit of path slot i; otherwise shadow ray i - n_ext.
+  auto begin = [&](uint32_t i, ctk::Walk& w) {
     if (i < n_ext) {
       const float4 ra = a.cur.a[i], rb = a.cur.b[i];
-      ctk::RayF r{ra.x, ra.y, ra.z, rb.x, rb.y, rb.z, ctk::kTMin, INFINITY, 0.0f, 0.0f, 0.0f};
-      ctk::finish_ray(r);
-      ctk::HitF h{-1, INFINITY, 0.0f, 0.0f};
-      if (a.scene.node_count > 0) ctk::walk_ordered<false>(a.scene, r, h, fallbacks);
-      a.hit_prim[i] = h.prim;
-      a.hit_t[i] = h.t;
+      w.r = ctk::RayF{ra.x, ra.y, ra.z, rb.x, rb.y, rb.z, ctk::kTMin, INFINITY, 0.0f, 0.0f, 0.0f};
     } else {
       const uint32_t j = i - n_ext;
       const float4 sa = a.shadow.a[j], sb = a.shadow.b[j];
-      ctk::RayF r{sa.x, sa.y, sa.z, sb.x, sb.y, sb.z, ctk::kTMin, sa.w, 0.0f, 0.0f, 0.0f};
-      ctk::finish_ray(r);
-      ctk::HitF h{-1, sa.w, 0.0f, 0.0f};
-      if (a.scene.node_count > 0) ctk::walk_ordered<true>(a.scene, r, h, fallbacks);
-      if (h.prim < 0) {
-        const float4 c = a.shadow.c[j];
-        float4* L = a.radiance + __float_as_uint(sb.w);
-        float4 l = *L;
-        l.x += c.x;
-        l.y += c.y;
-        l.z += c.z;
-        *L = l;
-      }
+      w.r = ctk::RayF{sa.x, sa.y, sa.z, sb.x, sb.y, sb.z, ctk::kTMin, sa.w, 0.0f, 0.0f, 0.0f};
+    }
+    ctk::finish_ray(w.r);
+    ctk::walk_begin(a.scene, w, i >= n_ext);
+  };
+  auto finish = [&](uint32_t i, ctk::Walk& w) {
+    if (i < n_ext) {
+      a.hit_prim[i] = w.h.prim;
+      a.hit_t[i] = w.h.t;
+    } else if (w.h.prim < 0) {  // unoccluded: add the NEE contribution
+      const uint32_t j = i - n_ext;
+      const float4 c = a.shadow.c[j];
+      float4* L = a.radiance + __float_as_uint(a.shadow.b[j].w);
+      float4 l = *L;
+      l.x += c.x;
+      l.y += c.y;
+      l.z += c.z;
+      *L = l;
+    }
+  };
+  if constexpr (PERSISTENT) {
+    ctk::walk_persistent(a.scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh, begin, finish,
+                         fallbacks);
+  } else {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_ext + n_sh; i += stride) {
+      ctk::Walk w;
+      begin(i, w);
+      while (w.ref != ctk::kWalkDone) ctk::walk_step(a.scene, w, fallbacks);
+      finish(i, w);
     }
   }
   if (fallbacks) atomicAdd(a.counts + 2 * a.max_bounces + 6, fallbacks);
@@ -322,14 +339,15 @@ int persistent_grid(K kernel) {
 }
 
 struct Grids {
-  int gen = 0, trace = 0, shade = 0, acc = 0;
+  int gen = 0, trace = 0, trace_persistent = 0, shade = 0, acc = 0;
 };
 
 const Grids& grids() {
   static Grids g = [] {
     Grids r;
     r.gen = persistent_grid(k_generate);
-    r.trace = persistent_grid(k_trace);
+    r.trace = persistent_grid(k_trace<false>);
+    r.trace_persistent = persistent_grid(k_trace<true>);
     r.shade = persistent_grid(k_shade);
     r.acc = persistent_grid(k_accumulate);
     return r;
@@ -372,7 +390,9 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   // Layout of the path buffer: 2 queues + shadow queue (3 float4 each per
   // path), radiance (float4), hit prim/t, counters.
   const size_t q_bytes = cap * sizeof(float4);
-  const size_t counter_words = 2 * (size_t)B + 8;
+  // [0, B+2) path queue sizes, [B+2, 2B+4) shadow queue sizes, 2B+6 fp64
+  // fallbacks, [2B+8, 3B+10) work counters of the persistent trace launches.
+  const size_t counter_words = 3 * (size_t)B + 12;
   const size_t bytes = 10 * q_bytes + cap * 8 + counter_words * 4 + 16 * 256;
   ct_status st = s->paths.buf.reserve(bytes, &s->device_bytes);
   if (st != CT_OK) return st;
@@ -405,6 +425,15 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   }
   a.sky_strength = (float)s->sky.strength;
   const Grids& g = grids();
+  // Deep trees make walk lengths uneven: refill lanes from a work counter.
+  const bool persistent = s->depth > kPersistentDepth;
+  auto trace = [&](const WaveArgs& w, int32_t b) {
+    ProfScope ps("trace", stream);
+    if (persistent)
+      k_trace<true><<<g.trace_persistent, kBlock, 0, stream>>>(w, b);
+    else
+      k_trace<false><<<g.trace, kBlock, 0, stream>>>(w, b);
+  };
   for (uint64_t done = 0; done < passes; done += per_wave) {
     const uint32_t p = (uint32_t)std::min<uint64_t>(per_wave, passes - done);
     a.paths = (uint32_t)(p * pixels);
@@ -416,20 +445,14 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
     }
     WaveArgs w = a;
     for (int32_t b = 0; b <= B; b++) {
-      {
-        ProfScope ps("trace", stream);
-        k_trace<<<g.trace, kBlock, 0, stream>>>(w, b);
-      }
+      trace(w, b);
       {
         ProfScope ps("shade", stream);
         k_shade<<<g.shade, kBlock, 0, stream>>>(w, b);
       }
       std::swap(w.cur, w.next);
     }
-    {
-      ProfScope ps("trace", stream);
-      k_trace<<<g.trace, kBlock, 0, stream>>>(w, B + 1);
-    }
+    trace(w, B + 1);
     {
       ProfScope ps("accumulate", stream);
       k_accumulate<<<g.acc, kBlock, 0, stream>>>(a.radiance, a.pixels, p, accum, sumsq);

@@ -1,12 +1,15 @@
 // Batched ray queries: intersectClosest (intersect.ts:202-282) and occluded
 // (intersect.ts:368-420) over device-resident scenes.
 //
-// One thread per ray in a grid-stride loop sized to the resident capacity of
-// the 152 SMs. A ray is two float4 loads (32 B); results are written with
-// coalesced 4-byte stores.
+// The ordered walk runs as persistent warps sized to the resident capacity of
+// the 152 SMs; lanes take rays from a work counter as their walks finish, so
+// uneven walk lengths do not idle the rest of the warp. A ray is two float4
+// loads (32 B). Closest hits whose float32 distance bound is loose are
+// flagged and recomputed in float64 by a separate, converged pass.
 #include <atomic>
 #include <cstring>
 
+#include "profile.hpp"
 #include "scene.hpp"
 
 namespace ct {
@@ -16,7 +19,7 @@ namespace {
 std::atomic<int32_t> g_variant{0};  // 0 ordered short-stack walk, 1 stackless skip links
 
 template <int VARIANT, bool ANY>
-__global__ void __launch_bounds__(128) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
+__global__ void __launch_bounds__(128, 8) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
                                                uint32_t n, int32_t* __restrict__ prim,
                                                float* __restrict__ t_out, float* __restrict__ u_out,
                                                float* __restrict__ v_out,
@@ -24,29 +27,67 @@ __global__ void __launch_bounds__(128) k_trace(ctk::SceneDev s, const float4* __
                                                uint32_t* __restrict__ counters) {
   uint32_t fallbacks = 0;
   bool overflow = false;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+  auto load = [&](uint32_t i, ctk::RayF& r) {
     const float4 r0 = __ldg(rays + 2 * (size_t)i), r1 = __ldg(rays + 2 * (size_t)i + 1);
-    ctk::RayF r{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, 0.0f, 0.0f, 0.0f};
+    r = ctk::RayF{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, 0.0f, 0.0f, 0.0f};
     ctk::finish_ray(r);
-    ctk::HitF h{-1, r.tmax, 0.0f, 0.0f};
-    if (s.node_count > 0) {
-      if (VARIANT == 0)
-        overflow |= !ctk::walk_ordered<ANY>(s, r, h, fallbacks);
-      else
-        ctk::walk_stackless<ANY>(s, r, h, fallbacks);
-    }
+  };
+  // A hit whose float32 distance is looser than ~3 ulp is stored with a
+  // negative t; k_refine replaces it with the reference's float64 value.
+  auto store = [&](uint32_t i, const ctk::RayF& r, ctk::HitF& h) {
     if (ANY) {
       blocked[i] = h.prim >= 0 ? 1 : 0;
     } else {
       prim[i] = h.prim;
-      t_out[i] = h.prim >= 0 ? h.t : INFINITY;
+      t_out[i] = h.prim < 0 ? INFINITY : (h.err > 2e-7f * h.t ? -h.t : h.t);
       if (u_out) u_out[i] = h.prim >= 0 ? h.u : 0.0f;
       if (v_out) v_out[i] = h.prim >= 0 ? h.v : 0.0f;
+    }
+  };
+  if (VARIANT == 0) {
+    ctk::walk_persistent(
+        s, counters + kCountQueue, n,
+        [&](uint32_t i, ctk::Walk& w) {
+          load(i, w.r);
+          ctk::walk_begin(s, w, ANY);
+        },
+        [&](uint32_t i, ctk::Walk& w) {
+          overflow |= w.overflow;
+          store(i, w.r, w.h);
+        },
+        fallbacks);
+  } else {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+      ctk::RayF r;
+      load(i, r);
+      ctk::HitF h{-1, r.tmax, 0.0f, 0.0f, 0.0f};
+      ctk::walk_stackless(s, r, h, ANY, fallbacks);
+      store(i, r, h);
     }
   }
   if (fallbacks) atomicAdd(&counters[kCountFallbacks], fallbacks);
   if (overflow) atomicOr(&counters[kCountError], 1u);
+}
+
+// Recomputes the flagged (negative) distances of closest hits in float64, in
+// the reference's operation order, with every lane of a warp in step.
+__global__ void __launch_bounds__(256) k_refine(ctk::SceneDev s, const float4* __restrict__ rays, uint32_t n,
+                                                const int32_t* __restrict__ prim, float* __restrict__ t_out,
+                                                float* __restrict__ u_out, float* __restrict__ v_out) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    if (!(t_out[i] < 0.0f)) continue;
+    const float4 r0 = __ldg(rays + 2 * (size_t)i), r1 = __ldg(rays + 2 * (size_t)i + 1);
+    ctk::RayF r{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, 0.0f, 0.0f, 0.0f};
+    ctk::HitF h{prim[i], -t_out[i], 0.0f, 0.0f, 1.0f};
+    if (u_out) h.u = u_out[i];
+    if (v_out) h.v = v_out[i];
+    ctk::refine_hit(s, r, h);
+    t_out[i] = h.t;
+    if (u_out) u_out[i] = h.u;
+    if (v_out) v_out[i] = h.v;
+  }
 }
 
 template <int VARIANT, bool ANY>
@@ -72,11 +113,30 @@ ct_status launch(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, floa
   const int variant = (g_variant.load() == 1 || s->depth > ctk::kStackSize) ? 1 : 0;
   const float4* r4 = reinterpret_cast<const float4*>(rays);
   uint32_t* cnt = s->counters.as<uint32_t>();
-  if (variant == 0)
-    k_trace<0, ANY><<<grid_for<0, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
-  else
-    k_trace<1, ANY><<<grid_for<1, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+  CT_CUDA(cudaMemsetAsync(cnt + kCountQueue, 0, sizeof(uint32_t), stream));  // persistent work counter
+  {
+    ProfScope ps(ANY ? "occluded" : "closest", stream);
+    if (variant == 0)
+      k_trace<0, ANY><<<grid_for<0, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+    else
+      k_trace<1, ANY><<<grid_for<1, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+  }
   CT_CUDA(cudaGetLastError());
+  if (!ANY) {
+    static int refine_grid = 0;
+    if (!refine_grid) {
+      int dev = 0, sms = 0, per_sm = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine, 256, 0);
+      refine_grid = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    ProfScope ps("refine", stream);
+    const uint64_t need = ((uint64_t)n + 255) / 256;
+    k_refine<<<(int)(need < (uint64_t)refine_grid ? need : refine_grid), 256, 0, stream>>>(s->dev, r4, n, prim, t,
+                                                                                           u, v);
+    CT_CUDA(cudaGetLastError());
+  }
   return CT_OK;
 }
 

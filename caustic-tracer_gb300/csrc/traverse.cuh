@@ -10,7 +10,7 @@
 // re-run in float64 with the reference's operation order and no FMA
 // contraction, which reproduces the reference's decision exactly. The
 // reported t then has a relative error below kTRel (else float64 too), so
-// two candidates can only swap order when their distances tie within 4e-6.
+// two candidates can only swap order when their distances tie within 8e-6.
 //
 // Box tests are float32 slab tests widened by 1+2*gamma(3) (Ize, "Robust BVH
 // Ray Traversal", JCGT 2013), so no box the float64 test enters is skipped.
@@ -24,7 +24,9 @@ namespace ctk {
 constexpr int kStackSize = 64;               // ordered-walk stack (tree depth is checked on upload)
 constexpr float kEps = 5.9604645e-8f;        // 2^-24
 constexpr float kErrK = 16.0f * kEps;        // error-bound multiplier (2x the first-order bound)
-constexpr float kTRel = 2e-6f;               // max relative error of a reported float32 t
+// Max relative error of a reported float32 t, checked against the first-order
+// bound (half of the kErrK bound): two hits swap order only within 8e-6.
+constexpr float kTRel = 4e-6f;
 constexpr float kBoxWiden = 1.0000005f;      // 1 + 2*gamma(3), rounded up
 
 // Device view of a scene. `pairs` holds one 64-byte record per interior node
@@ -114,12 +116,23 @@ static __device__ __noinline__ double sphere_exact(const RayF& r, float4 c4, flo
   return t;
 }
 
-// ---- float32 tests with exact fallback -------------------------------------
+// ---- float32 candidate tests with exact fallback ------------------------------
+//
+// A candidate is a primitive the ray hits inside its own (tmin, tmax). The
+// tests below classify in float32 when every decision is certain and return
+// t with a rigorous error bound `e`; otherwise they run the reference's
+// float64 test and return its t (e = the float32 rounding of that t).
+// Ordering candidates against the current closest hit happens in test_leaf.
 
-// Result of a primitive test: 0 miss, 1 hit (t/u/v written).
-__device__ __forceinline__ bool tri_test(const RayF& r, float4 a4, float4 b4, float4 c4,
-                                         float closest, float& t_out, float& u_out, float& v_out,
-                                         uint32_t& fallbacks) {
+struct Cand {
+  float t, e, u, v;
+};
+
+__device__ __forceinline__ float rounding_err(float t) { return fabsf(t) * kEps; }
+
+// intersect.ts:52-85. Returns true for a candidate.
+__device__ __forceinline__ bool tri_candidate(const RayF& r, float4 a4, float4 b4, float4 c4, Cand& c,
+                                              uint32_t& fallbacks) {
   const float e1x = b4.x - a4.x, e1y = b4.y - a4.y, e1z = b4.z - a4.z;
   const float e2x = c4.x - a4.x, e2y = c4.y - a4.y, e2z = c4.z - a4.z;
   const float px = r.dy * e2z - r.dz * e2y;
@@ -140,10 +153,9 @@ __device__ __forceinline__ bool tri_test(const RayF& r, float4 a4, float4 b4, fl
     if (ad + ed < 1e-12f) return false;  // |det| < 1e-12 for certain
     exact = true;
   }
-  const float sg = det < 0.0f ? -1.0f : 1.0f;
-  const float su = sg * un;
-  float sv = 0.0f, st = 0.0f, ev = 0.0f, et = 0.0f;
   if (!exact) {
+    const float sg = det < 0.0f ? -1.0f : 1.0f;
+    const float su = sg * un;
     if (su < -eu || su - ad > eu + ed) return false;  // u < 0 or u > 1 for certain
     if (fabsf(su) <= eu || fabsf(su - ad) <= eu + ed) {
       exact = true;
@@ -154,60 +166,56 @@ __device__ __forceinline__ bool tri_test(const RayF& r, float4 a4, float4 b4, fl
       const float qax = fabsf(ty * e1z) + fabsf(tz * e1y);
       const float qay = fabsf(tz * e1x) + fabsf(tx * e1z);
       const float qaz = fabsf(tx * e1y) + fabsf(ty * e1x);
-      sv = sg * (r.dx * qx + r.dy * qy + r.dz * qz);
-      ev = kErrK * (fabsf(r.dx) * qax + fabsf(r.dy) * qay + fabsf(r.dz) * qaz);
+      const float sv = sg * (r.dx * qx + r.dy * qy + r.dz * qz);
+      const float ev = kErrK * (fabsf(r.dx) * qax + fabsf(r.dy) * qay + fabsf(r.dz) * qaz);
       const float euv = eu + ev + ed;
       if (sv < -ev || su + sv - ad > euv) return false;  // v < 0 or u + v > 1
       if (fabsf(sv) <= ev || fabsf(su + sv - ad) <= euv) {
         exact = true;
       } else {
-        st = sg * (e2x * qx + e2y * qy + e2z * qz);
-        et = kErrK * (fabsf(e2x) * qax + fabsf(e2y) * qay + fabsf(e2z) * qaz);
+        const float st = sg * (e2x * qx + e2y * qy + e2z * qz);
+        const float et = kErrK * (fabsf(e2x) * qax + fabsf(e2y) * qay + fabsf(e2z) * qaz);
         const float mlo = et + r.tmin * ed;
-        const float dlo = st - r.tmin * ad;  // t - tmin, scaled by |det|
+        const float dlo = st - r.tmin * ad;  // (t - tmin) * |det|
         if (dlo < -mlo) return false;         // t <= tmin
-        if (fabsf(dlo) <= mlo) {
-          exact = true;
-        } else if (closest < INFINITY) {
-          const float mhi = et + closest * ed;
-          const float dhi = st - closest * ad;
-          if (dhi > mhi) return false;  // t >= closest
+        if (fabsf(dlo) <= mlo) exact = true;
+        if (!exact && r.tmax < INFINITY) {
+          const float mhi = et + r.tmax * ed;
+          const float dhi = st - r.tmax * ad;  // (t - tmax) * |det|
+          if (dhi > mhi) return false;          // t >= tmax
           if (fabsf(dhi) <= mhi) exact = true;
         }
         if (!exact) {
-          const float t = st / ad;
-          if (et + t * ed > kTRel * t * ad) {
-            exact = true;  // t not accurate enough for ordering
-          } else {
-            t_out = t;
-            u_out = su / ad;
-            v_out = sv / ad;
-            return true;
-          }
+          c.t = st / ad;
+          c.e = (et + c.t * ed) / ad + rounding_err(c.t);
+          c.u = su / ad;
+          c.v = sv / ad;
+          return true;
         }
       }
     }
   }
   fallbacks++;
   double t, u, v;
-  if (!tri_exact(r, a4, b4, c4, (double)r.tmin, (double)closest, &t, &u, &v)) return false;
-  t_out = (float)t;
-  u_out = (float)u;
-  v_out = (float)v;
+  if (!tri_exact(r, a4, b4, c4, (double)r.tmin, (double)r.tmax, &t, &u, &v)) return false;
+  c.t = (float)t;
+  c.e = rounding_err(c.t);
+  c.u = (float)u;
+  c.v = (float)v;
   return true;
 }
 
-// Sphere test; returns true and sets t_out when hit in (tmin, closest).
-__device__ __forceinline__ bool sphere_test(const RayF& r, float4 c4, float rad, float closest,
-                                            float& t_out, uint32_t& fallbacks) {
+// intersect.ts:20-39: near root if inside (tmin, tmax), else the far root.
+__device__ __forceinline__ bool sphere_candidate(const RayF& r, float4 c4, float rad, Cand& c,
+                                                 uint32_t& fallbacks) {
   const float lx = r.ox - c4.x, ly = r.oy - c4.y, lz = r.oz - c4.z;
   const float a = r.dx * r.dx + r.dy * r.dy + r.dz * r.dz;
   const float hb = lx * r.dx + ly * r.dy + lz * r.dz;
   const float ll = lx * lx + ly * ly + lz * lz;
-  const float c = ll - rad * rad;
-  const float disc = hb * hb - a * c;
+  const float disc = hb * hb - a * (ll - rad * rad);
   const float hba = fabsf(lx * r.dx) + fabsf(ly * r.dy) + fabsf(lz * r.dz);
   const float edisc = kErrK * (hba * hba + a * (ll + rad * rad));
+  c.u = c.v = 0.0f;
   bool exact = false;
   if (disc < -edisc) return false;
   if (disc <= edisc) {
@@ -217,152 +225,299 @@ __device__ __forceinline__ bool sphere_test(const RayF& r, float4 c4, float rad,
     const float es = edisc / s + kEps * s;
     const float ehb = kErrK * hba;
     const float inva = 1.0f / a;
-    // candidate roots, near first (intersect.ts:33-37)
-    for (int k = 0; k < 2 && !exact; k++) {
-      const float num = k == 0 ? -hb - s : -hb + s;
-      const float t = num * inva;
+    for (int k = 0; k < 2; k++) {
+      const float t = (k == 0 ? -hb - s : -hb + s) * inva;
       const float e = (ehb + es) * inva + kErrK * fabsf(t);
-      if (t + e <= r.tmin || t - e >= closest) continue;  // root rejected for certain
-      if (t - e > r.tmin && t + e < closest) {
-        if (e > kTRel * t) {
-          exact = true;
-          break;
-        }
-        t_out = t;
+      if (t + e <= r.tmin || t - e >= r.tmax) continue;  // root rejected for certain
+      if (t - e > r.tmin && t + e < r.tmax) {
+        c.t = t;
+        c.e = e + rounding_err(t);
         return true;
       }
       exact = true;
+      break;
     }
     if (!exact) return false;
   }
   fallbacks++;
-  const double t = sphere_exact(r, c4, rad, (double)r.tmin, (double)closest);
+  const double t = sphere_exact(r, c4, rad, (double)r.tmin, (double)r.tmax);
   if (!(t > 0)) return false;
-  t_out = (float)t;
+  c.t = (float)t;
+  c.e = rounding_err(c.t);
   return true;
-}
-
-// Conservative slab test against [lo, hi]; returns the entry distance or +inf.
-__device__ __forceinline__ float box_entry(const RayF& r, float lox, float hix, float loy,
-                                           float hiy, float loz, float hiz, float closest) {
-  const float tx0 = (lox - r.ox) * r.ix, tx1 = (hix - r.ox) * r.ix;
-  const float ty0 = (loy - r.oy) * r.iy, ty1 = (hiy - r.oy) * r.iy;
-  const float tz0 = (loz - r.oz) * r.iz, tz1 = (hiz - r.oz) * r.iz;
-  const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-  const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1)) * kBoxWiden;
-  return (tn <= tf && tf >= 0.0f && tn <= closest) ? tn : INFINITY;
 }
 
 struct HitF {
   int32_t prim;
   float t, u, v;
+  float err;  // bound on |t - reference t| for the current closest hit
 };
 
-// Tests the primitives of a leaf (intersect.ts:155-193). ANY: stop at the first hit.
-template <bool ANY>
-__device__ __forceinline__ bool test_leaf(const SceneDev& s, const RayF& r, uint32_t leafword,
-                                          HitF& h, uint32_t& fallbacks) {
-  const uint32_t count = leafword & 7u, start = leafword >> 3;
-  for (uint32_t p = start; p < start + count; p++) {
-    const float4* q = s.prims + (size_t)p * 4;
-    const float4 a4 = __ldg(q);
-    const float4 b4 = __ldg(q + 1);
-    float t, u = 0.0f, v = 0.0f;
-    bool hit;
-    if (a4.w == 0.0f) {
-      hit = sphere_test(r, a4, b4.x, h.t, t, fallbacks);
+// float64 distance of `prim` along the ray (the reference's value), or -1.
+static __device__ __noinline__ double exact_t(const SceneDev& s, const RayF& r, int32_t prim) {
+  const float4* q = s.prims + (size_t)prim * 4;
+  const float4 a4 = __ldg(q), b4 = __ldg(q + 1);
+  if (a4.w == 0.0f) return sphere_exact(r, a4, b4.x, (double)r.tmin, (double)r.tmax);
+  double t, u, v;
+  return tri_exact(r, a4, b4, __ldg(q + 2), (double)r.tmin, (double)r.tmax, &t, &u, &v) ? t : -1.0;
+}
+
+// Replaces a closest hit whose float32 distance is looser than ~3 ulp by the
+// reference's float64 t (and barycentrics), once per ray after the walk.
+static __device__ __noinline__ void refine_hit(const SceneDev& s, const RayF& r, HitF& h) {
+  const float4* q = s.prims + (size_t)h.prim * 4;
+  const float4 a4 = __ldg(q), b4 = __ldg(q + 1);
+  if (a4.w == 0.0f) {
+    const double t = sphere_exact(r, a4, b4.x, (double)r.tmin, (double)r.tmax);
+    if (t > 0) h.t = (float)t;
+  } else {
+    double t, u, v;
+    if (tri_exact(r, a4, b4, __ldg(q + 2), (double)r.tmin, (double)r.tmax, &t, &u, &v)) {
+      h.t = (float)t;
+      h.u = (float)u;
+      h.v = (float)v;
+    }
+  }
+  h.err = rounding_err(h.t);
+}
+
+__device__ __forceinline__ void finish_hit(const SceneDev& s, const RayF& r, HitF& h) {
+  if (h.prim >= 0 && h.err > 2e-7f * h.t) refine_hit(s, r, h);
+}
+
+// Tests one primitive of a leaf (intersect.ts:155-193). A candidate replaces
+// the closest hit when it is nearer by more than both error bounds; when the
+// two distances overlap within their bounds and the bounds are small (a tie
+// within 1e-5), the float32 order decides; otherwise both distances are
+// recomputed in float64 and compared exactly like the reference.
+// any: returns true for any candidate (occlusion).
+__device__ __forceinline__ bool test_prim(const SceneDev& s, const RayF& r, uint32_t p, HitF& h, bool any,
+                                          uint32_t& fallbacks) {
+  const float4* q = s.prims + (size_t)p * 4;
+  const float4 a4 = __ldg(q);
+  const float4 b4 = __ldg(q + 1);
+  Cand c;
+  const bool cand = a4.w == 0.0f ? sphere_candidate(r, a4, b4.x, c, fallbacks)
+                                 : tri_candidate(r, a4, b4, __ldg(q + 2), c, fallbacks);
+  if (!cand) return false;
+  if (any) {
+    h.prim = (int32_t)p;
+    h.t = c.t;
+    return true;
+  }
+  bool take;
+  if (h.prim < 0 || c.t + c.e < h.t - h.err) {
+    take = true;
+  } else if (c.t - c.e > h.t + h.err) {
+    take = false;
+  } else if (c.e + h.err <= 5e-6f * fminf(c.t, h.t)) {
+    take = c.t < h.t;  // a tie within 1e-5: either order is admissible
+  } else {
+    fallbacks += 2;
+    const double tn = exact_t(s, r, (int32_t)p), tb = exact_t(s, r, h.prim);
+    take = tn < tb;
+    if (take) {
+      c.t = (float)tn;
+      c.e = rounding_err(c.t);
     } else {
-      const float4 c4 = __ldg(q + 2);
-      hit = tri_test(r, a4, b4, c4, h.t, t, u, v, fallbacks);
+      h.t = (float)tb;
+      h.err = rounding_err(h.t);
     }
-    if (hit) {
-      h.t = t;
-      h.prim = (int32_t)p;
-      h.u = u;
-      h.v = v;
-      if (ANY) return true;
-    }
+  }
+  if (take) {
+    h.prim = (int32_t)p;
+    h.t = c.t;
+    h.err = c.e;
+    h.u = c.u;
+    h.v = c.v;
   }
   return false;
 }
 
+// All primitives of a leaf; returns true at the first candidate when `any`.
+__device__ __forceinline__ bool test_leaf(const SceneDev& s, const RayF& r, uint32_t leafword, HitF& h, bool any,
+                                          uint32_t& fallbacks) {
+  const uint32_t count = leafword & 7u, start = leafword >> 3;
+  for (uint32_t p = start; p < start + count; p++)
+    if (test_prim(s, r, p, h, any, fallbacks)) return true;
+  return false;
+}
+
+// Conservative slab test against [lo, hi]; returns the entry distance or +inf.
+__device__ __forceinline__ float box_entry(const RayF& r, float lox, float hix, float loy,
+                                           float hiy, float loz, float hiz, float bound) {
+  const float tx0 = (lox - r.ox) * r.ix, tx1 = (hix - r.ox) * r.ix;
+  const float ty0 = (loy - r.oy) * r.iy, ty1 = (hiy - r.oy) * r.iy;
+  const float tz0 = (loz - r.oz) * r.iz, tz1 = (hiz - r.oz) * r.iz;
+  const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+  const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1)) * kBoxWiden;
+  return (tn <= tf && tf >= 0.0f && tn <= bound) ? tn : INFINITY;
+}
+
+// Upper bound of the reference's current closest distance (prunes boxes).
+__device__ __forceinline__ float prune_bound(const HitF& h) { return h.t + h.err; }
+
 // Ordered front-to-back walk over the interior pair records (the reference's
-// intersectClosest, intersect.ts:202-282). ANY = any-hit for occlusion
-// (intersect.ts:368-420). h.t must hold the ray's tmax on entry. Returns
-// false if the stack would overflow (never for trees that passed the upload
-// depth check); no out-of-bounds write happens in that case.
-template <bool ANY>
-__device__ __forceinline__ bool walk_ordered(const SceneDev& s, const RayF& r, HitF& h,
-                                             uint32_t& fallbacks) {
-  if (box_entry(r, s.root_lo[0], s.root_hi[0], s.root_lo[1], s.root_hi[1], s.root_lo[2],
-                s.root_hi[2], h.t) == INFINITY)
-    return true;
+// intersectClosest, intersect.ts:202-282; with `any`, the any-hit query of
+// occluded, intersect.ts:368-420), as a state machine advanced one step at a
+// time: a step expands one interior record (both child boxes, nearer child
+// first, farther child pushed with its entry distance), tests one primitive of
+// the current leaf, or pops the stack past entries beyond the closest hit.
+// Equal-cost steps keep the lanes of a warp in step with each other.
+struct Walk {
+  RayF r;
+  HitF h;
+  int32_t ref;           // >= 0 interior record, kLeaf: testing [cur, end), kPop, kDone
+  uint32_t cur, end;
+  int32_t sp;
+  bool any, overflow;
   int32_t stack_ref[kStackSize];
   float stack_t[kStackSize];
-  int sp = 0;
-  int32_t ref = s.root_ref;
-  for (;;) {
-    while (ref >= 0) {
-      const float4* pr = s.pairs + (size_t)ref * 4;
-      const float4 n0 = __ldg(pr), n1 = __ldg(pr + 1), n2 = __ldg(pr + 2), n3 = __ldg(pr + 3);
-      const float tl = box_entry(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, h.t);
-      const float tr = box_entry(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, h.t);
-      const int32_t cl = __float_as_int(n3.x), cr = __float_as_int(n3.y);
-      if (tl != INFINITY) {
-        if (tr != INFINITY) {
-          if (sp >= kStackSize) return false;
-          if (tl <= tr) {
-            stack_ref[sp] = cr;
-            stack_t[sp++] = tr;
-            ref = cl;
-          } else {
-            stack_ref[sp] = cl;
-            stack_t[sp++] = tl;
-            ref = cr;
-          }
-        } else {
-          ref = cl;
-        }
-        continue;
-      }
-      if (tr != INFINITY) {
-        ref = cr;
-        continue;
-      }
-      ref = INT32_MAX;  // no child entered: pop
-      break;
-    }
-    if (ref != INT32_MAX) {
-      if (test_leaf<ANY>(s, r, (uint32_t)~ref, h, fallbacks)) return true;
-    }
-    // pop entries still closer than the current hit
-    for (;;) {
-      if (sp == 0) return true;
-      --sp;
-      if (stack_t[sp] < h.t) break;
-    }
-    ref = stack_ref[sp];
+};
+
+constexpr int32_t kWalkPop = INT32_MAX, kWalkDone = INT32_MIN, kWalkLeaf = INT32_MIN + 1;
+
+// Starts a walk for w.r (tmin/tmax set, inverse direction computed).
+__device__ __forceinline__ void walk_begin(const SceneDev& s, Walk& w, bool any) {
+  w.h = HitF{-1, w.r.tmax, 0.0f, 0.0f, 0.0f};
+  w.sp = 0;
+  w.any = any;
+  w.overflow = false;
+  w.ref = (s.node_count == 0 || box_entry(w.r, s.root_lo[0], s.root_hi[0], s.root_lo[1], s.root_hi[1],
+                                          s.root_lo[2], s.root_hi[2], w.r.tmax) == INFINITY)
+              ? kWalkDone : s.root_ref;
+  if (w.ref < 0 && w.ref != kWalkDone) {  // the root is a leaf
+    const uint32_t word = (uint32_t)~w.ref;
+    w.cur = word >> 3;
+    w.end = w.cur + (word & 7u);
+    w.ref = w.cur < w.end ? kWalkLeaf : kWalkDone;
   }
+}
+
+// Enters child `c` (interior record or ~leafword).
+__device__ __forceinline__ void walk_enter(Walk& w, int32_t c) {
+  if (c >= 0) {
+    w.ref = c;
+  } else {
+    const uint32_t word = (uint32_t)~c;
+    w.cur = word >> 3;
+    w.end = w.cur + (word & 7u);
+    w.ref = w.cur < w.end ? kWalkLeaf : kWalkPop;
+  }
+}
+
+// One step; w.ref == kWalkDone when the query is answered.
+__device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& fallbacks) {
+  if (w.ref == kWalkLeaf) {
+    if (test_prim(s, w.r, w.cur, w.h, w.any, fallbacks)) {
+      w.ref = kWalkDone;
+      return;
+    }
+    if (++w.cur == w.end) w.ref = kWalkPop;
+  } else if (w.ref >= 0 && w.ref != kWalkPop) {
+    const float4* pr = s.pairs + (size_t)w.ref * 4;
+    const float4 n0 = __ldg(pr), n1 = __ldg(pr + 1), n2 = __ldg(pr + 2), n3 = __ldg(pr + 3);
+    const float bound = prune_bound(w.h);
+    const float tl = box_entry(w.r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, bound);
+    const float tr = box_entry(w.r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, bound);
+    const int32_t cl = __float_as_int(n3.x), cr = __float_as_int(n3.y);
+    if (tl != INFINITY && tr != INFINITY) {
+      if (w.sp >= kStackSize) {
+        w.overflow = true;
+        w.ref = kWalkDone;
+        return;
+      }
+      const bool left_first = tl <= tr;
+      w.stack_ref[w.sp] = left_first ? cr : cl;
+      w.stack_t[w.sp++] = left_first ? tr : tl;
+      walk_enter(w, left_first ? cl : cr);
+    } else if (tl != INFINITY || tr != INFINITY) {
+      walk_enter(w, tl != INFINITY ? cl : cr);
+    } else {
+      w.ref = kWalkPop;
+    }
+  }
+  if (w.ref == kWalkPop) {
+    w.ref = kWalkDone;
+    const float bound = prune_bound(w.h);
+    while (w.sp > 0) {
+      --w.sp;
+      if (w.stack_t[w.sp] <= bound) {
+        walk_enter(w, w.stack_ref[w.sp]);
+        break;
+      }
+    }
+  }
+}
+
+// Persistent warp loop over `total` queries numbered 0..total-1, handed out in
+// warp-sized batches from *counter. begin(i, w) loads query i into w.r and
+// calls walk_begin; finish(i, w) consumes the answer. A lane whose query is
+// answered is refilled as soon as a quarter of the warp is idle, so lanes
+// keep stepping instead of waiting for the warp's slowest ray. All 32 lanes
+// of every warp must call this (the block size is a multiple of 32).
+template <class Begin, class Finish>
+__device__ __forceinline__ void walk_persistent(const SceneDev& s, uint32_t* counter, uint32_t total, Begin begin,
+                                                Finish finish, uint32_t& fallbacks) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  Walk w;
+  w.ref = kWalkDone;
+  int64_t idx = -1;  // query held by this lane
+  bool drained = false;
+  for (;;) {
+    const bool idle = w.ref == kWalkDone;
+    if (idle && idx >= 0) {
+      finish((uint32_t)idx, w);
+      idx = -1;
+    }
+    const uint32_t want = __ballot_sync(0xffffffffu, idle);
+    if (!drained && (__popc(want) >= 8 || want == 0xffffffffu)) {
+      const uint32_t leader = __ffs(want) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + __popc(want) >= total) drained = true;
+      if (idle) {
+        const uint32_t k = base + __popc(want & lt_mask);
+        if (k < total) {
+          idx = k;
+          begin(k, w);
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, idx < 0) && drained) break;
+    if (w.ref != kWalkDone) walk_step(s, w, fallbacks);
+  }
+}
+
+// Complete walk of one query in the calling thread (no refill).
+__device__ __forceinline__ bool walk_ordered(const SceneDev& s, const RayF& r, HitF& h, bool any,
+                                             uint32_t& fallbacks) {
+  Walk w;
+  w.r = r;
+  walk_begin(s, w, any);
+  while (w.ref != kWalkDone) walk_step(s, w, fallbacks);
+  h = w.h;
+  return !w.overflow;
 }
 
 // Stackless skip-link walk over the reference node array, the literal
 // mirror of intersectClosestStackless (intersect.ts:290-365) and occluded
 // (intersect.ts:368-420).
-template <bool ANY>
-__device__ __forceinline__ void walk_stackless(const SceneDev& s, const RayF& r, HitF& h,
+__device__ __forceinline__ void walk_stackless(const SceneDev& s, const RayF& r, HitF& h, bool any,
                                                uint32_t& fallbacks) {
   uint32_t node = 0;
   while (node < s.node_count) {
     const float4 lo = __ldg(s.nodes + (size_t)node * 2);
     const float4 hi = __ldg(s.nodes + (size_t)node * 2 + 1);
-    if (box_entry(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, h.t) == INFINITY) {
+    if (box_entry(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, prune_bound(h)) == INFINITY) {
       node = (uint32_t)lo.w;
-      continue;
+    } else if (hi.w >= 0.0f && test_leaf(s, r, (uint32_t)hi.w, h, any, fallbacks) && any) {
+      node = s.node_count;
+    } else {
+      node++;
     }
-    if (hi.w >= 0.0f) {
-      if (test_leaf<ANY>(s, r, (uint32_t)hi.w, h, fallbacks)) return;
-    }
-    node++;
   }
 }
 
