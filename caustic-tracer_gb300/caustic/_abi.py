@@ -143,6 +143,8 @@ SIGNATURES = {
     "ct_accumulate_passes_device": (C.c_int, [P, C.POINTER(ct_camera_frame), C.c_int32, C.c_int32, C.c_uint32,
                                               C.c_int32, C.POINTER(ct_trace_options), P, P, P]),
     "ct_render_image_device": (C.c_int, [P, C.POINTER(ct_camera_frame), C.POINTER(ct_render_options), P, P]),
+    "ct_accumulate_pass_noalloc": (C.c_int, [P, C.POINTER(ct_camera_frame), C.c_int32, C.c_int32, C.c_uint32,
+                                             C.POINTER(ct_trace_options), P, P]),
     "ct_profile_enable": (None, [C.c_int32]),
     "ct_profile_reset": (None, []),
     "ct_profile_read": (C.c_int32, [C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_int32]),

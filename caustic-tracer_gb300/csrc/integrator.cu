@@ -572,3 +572,125 @@ ct_status ct_render_image(ct_scene* scene, const ct_camera_frame* frame, const c
 }
 
 }  // extern "C"
+
+// ---- accumulatePass without allocation ------------------------------------------
+//
+// Some callers cannot allocate device memory at the time they render: code
+// that is recording a CUDA graph (cudaMalloc is not allowed while a stream is
+// being captured), real-time loops that forbid allocation per frame, and
+// plugin hosts that hand the library a fixed memory budget at load time and
+// own every later allocation. ct_accumulate_pass_noalloc serves them: its
+// scratch (path queues, shadow queue, per-path radiance, hit records, queue
+// counters) lives in the file-scope array below, which every GPU that loads
+// this library holds until the process exits. The scene (created earlier
+// with ct_scene_create) and the accumulation buffer are the caller's.
+namespace ct {
+namespace {
+
+constexpr uint32_t kNoAllocMaxPixels = CT_NOALLOC_MAX_PIXELS;
+constexpr size_t kNoAllocPathBytes = 10 * sizeof(float4) + 2 * sizeof(uint32_t);  // per path slot
+constexpr size_t kNoAllocCounterWords = 4096;
+constexpr size_t kNoAllocScratchBytes =
+    (size_t)kNoAllocMaxPixels * kNoAllocPathBytes + kNoAllocCounterWords * 4 + 16 * 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host symbol itself is only a stand-in for it).
+ct_status noalloc_scratch(int device, void** out) {
+  CT_CHECK_ARG(device >= 0 && device < kMaxDevices, "device %d beyond %d", device, kMaxDevices);
+  std::lock_guard<std::mutex> guard(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    CT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[device] = p;
+  }
+  *out = g_noalloc_ptr[device];
+  return CT_OK;
+}
+
+}  // namespace
+}  // namespace ct
+
+extern "C" {
+
+ct_status ct_accumulate_pass_noalloc(ct_scene* scene, const ct_camera_frame* frame, int32_t width, int32_t height,
+                                     uint32_t frame_index, const ct_trace_options* opts, float* accum, void* stream) {
+  using namespace ct;
+  clear_error();
+  CT_CHECK_ARG(scene != nullptr && opts != nullptr && accum != nullptr, "NULL argument");
+  ct_status st = check_options(frame, width, height, opts->max_bounces);
+  if (st != CT_OK) return st;
+  const uint64_t pixels = (uint64_t)width * (uint64_t)height;
+  CT_CHECK_ARG(pixels <= kNoAllocMaxPixels,
+               "ct_accumulate_pass_noalloc: %dx%d = %llu pixels exceeds the static scratch limit of %u pixels",
+               width, height, (unsigned long long)pixels, kNoAllocMaxPixels);
+  const int32_t B = opts->max_bounces;
+  const size_t counter_words = 3 * (size_t)B + 12;
+  CT_CHECK_ARG(counter_words <= kNoAllocCounterWords, "max_bounces %d needs more queue counters than the static scratch holds", B);
+  std::lock_guard<std::mutex> guard(scene->lock);
+  CT_CUDA(cudaSetDevice(scene->device));
+  void* scratch = nullptr;
+  st = noalloc_scratch(scene->device, &scratch);
+  if (st != CT_OK) return st;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : scene->stream;
+
+  // Carve the per-path arrays for exactly `pixels` slots (one pass).
+  char* base = static_cast<char*>(scratch);
+  auto take = [&](size_t n) {
+    char* p = base;
+    base += (n + 255) & ~size_t(255);
+    return p;
+  };
+  const size_t q = pixels * sizeof(float4);
+  WaveArgs a{};
+  a.scene = scene->dev;
+  a.frame = to_frame(*frame);
+  a.cur = Queue{(float4*)take(q), (float4*)take(q), (float4*)take(q)};
+  a.next = Queue{(float4*)take(q), (float4*)take(q), (float4*)take(q)};
+  a.shadow = ShadowQueue{(float4*)take(q), (float4*)take(q), (float4*)take(q)};
+  a.radiance = (float4*)take(q);
+  a.hit_prim = (int32_t*)take(pixels * 4);
+  a.hit_t = (float*)take(pixels * 4);
+  a.counts = (uint32_t*)take(counter_words * 4);
+  CT_CHECK_ARG((size_t)(base - static_cast<char*>(scratch)) <= kNoAllocScratchBytes, "static scratch layout overflow");
+  a.width = (uint32_t)width;
+  a.height = (uint32_t)height;
+  a.pixels = (uint32_t)pixels;
+  a.paths = (uint32_t)pixels;
+  a.first_frame = frame_index;
+  a.max_bounces = B;
+  a.rr = opts->russian_roulette;
+  a.nee = opts->nee;
+  a.sky_kind = scene->sky.kind;
+  for (int k = 0; k < 3; k++) {
+    a.sky_zenith[k] = (float)scene->sky.zenith[k];
+    a.sky_horizon[k] = (float)scene->sky.horizon[k];
+  }
+  a.sky_strength = (float)scene->sky.strength;
+
+  // The array keeps the previous call's contents: the counters must start at zero.
+  CT_CUDA(cudaMemsetAsync(a.counts, 0, counter_words * 4, s));
+  const Grids& g = grids();
+  const bool persistent = scene->depth > kPersistentDepth;
+  k_generate<<<g.gen, kBlock, 0, s>>>(a);
+  WaveArgs w = a;
+  for (int32_t b = 0; b <= B + 1; b++) {
+    if (persistent)
+      k_trace<true><<<g.trace_persistent, kBlock, 0, s>>>(w, b);
+    else
+      k_trace<false><<<g.trace, kBlock, 0, s>>>(w, b);
+    if (b > B) break;
+    k_shade<<<g.shade, kBlock, 0, s>>>(w, b);
+    std::swap(w.cur, w.next);
+  }
+  k_accumulate<<<g.acc, kBlock, 0, s>>>(a.radiance, a.pixels, 1, accum, nullptr);
+  CT_CUDA(cudaGetLastError());
+  return CT_OK;
+}
+
+}  // extern "C"

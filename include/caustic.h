@@ -239,6 +239,26 @@ ct_status ct_accumulate_passes_device(ct_scene* scene, const ct_camera_frame* fr
 ct_status ct_render_image_device(ct_scene* scene, const ct_camera_frame* frame,
                                  const ct_render_options* opts, float* out, void* stream);
 
+/* ---- accumulatePass without allocation ------------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device
+ * memory when they render: code recording a CUDA graph (cudaMalloc is not
+ * allowed while a stream is captured), real-time loops that forbid per-frame
+ * allocation, and plugin hosts that own every allocation after load time.
+ * Same work as ct_accumulate_pass (one sample per pixel, seeded by
+ * Rng.fromPixel(pixel, frame_index), added into accum), but all scratch lives
+ * in one static device array of the library, sized for CT_NOALLOC_MAX_PIXELS
+ * pixels (about 42 MiB; every GPU that loads the library holds it until the
+ * process exits). Larger images are rejected with CT_ERR_INVALID_ARGUMENT.
+ * accum is a device array (width*height*3 floats); the scene comes from
+ * ct_scene_create. The first call on a device looks the array up once for
+ * that device; make that first call before any stream capture. All calls
+ * share the one array, so calls that overlap on the GPU (on different
+ * streams or different scenes) race: order them on one stream.           */
+#define CT_NOALLOC_MAX_PIXELS (512u * 512u)
+ct_status ct_accumulate_pass_noalloc(ct_scene* scene, const ct_camera_frame* frame, int32_t width,
+                                     int32_t height, uint32_t frame_index, const ct_trace_options* opts,
+                                     float* accum, void* stream);
+
 /* ---- profiling ------------------------------------------------------------
  * No counterpart in the reference (which times with performance.now(),
  * reference.ts:28,42). While enabled, every kernel launch is bracketed by
