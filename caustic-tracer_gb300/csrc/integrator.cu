@@ -155,14 +155,14 @@ __global__ void __launch_bounds__(kBlock, 8) k_trace(WaveArgs a, int32_t bounce)
     }
   };
   if constexpr (PERSISTENT) {
-    ctk::walk_persistent(a.scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh, begin, finish,
+    ctk::walk_persistent<false>(a.scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh, begin, finish,
                          fallbacks);
   } else {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_ext + n_sh; i += stride) {
       ctk::Walk w;
       begin(i, w);
-      while (w.ref != ctk::kWalkDone) ctk::walk_step(a.scene, w, fallbacks);
+      while (w.ref != ctk::kWalkDone) ctk::walk_step<false>(a.scene, w, fallbacks);
       finish(i, w);
     }
   }

@@ -285,18 +285,76 @@ __device__ __forceinline__ void finish_hit(const SceneDev& s, const RayF& r, Hit
   if (h.prim >= 0 && h.err > 2e-7f * h.t) refine_hit(s, r, h);
 }
 
-// Tests one primitive of a leaf (intersect.ts:155-193). A candidate replaces
-// the closest hit when it is nearer by more than both error bounds; when the
-// two distances overlap within their bounds and the bounds are small (a tie
-// within 1e-5), the float32 order decides; otherwise both distances are
-// recomputed in float64 and compared exactly like the reference.
+// Plain float32 forms of the reference's tests (same decisions, float32
+// rounding), for the path integrator whose parity is statistical. The
+// candidate must also be nearer than `closest`.
+__device__ __forceinline__ bool tri_fast(const RayF& r, float4 a4, float4 b4, float4 c4, float closest, Cand& c) {
+  const float e1x = b4.x - a4.x, e1y = b4.y - a4.y, e1z = b4.z - a4.z;
+  const float e2x = c4.x - a4.x, e2y = c4.y - a4.y, e2z = c4.z - a4.z;
+  const float px = r.dy * e2z - r.dz * e2y;
+  const float py = r.dz * e2x - r.dx * e2z;
+  const float pz = r.dx * e2y - r.dy * e2x;
+  const float det = e1x * px + e1y * py + e1z * pz;
+  if (det > -1e-12f && det < 1e-12f) return false;
+  const float inv = 1.0f / det;
+  const float tx = r.ox - a4.x, ty = r.oy - a4.y, tz = r.oz - a4.z;
+  const float u = (tx * px + ty * py + tz * pz) * inv;
+  if (u < 0.0f || u > 1.0f) return false;
+  const float qx = ty * e1z - tz * e1y;
+  const float qy = tz * e1x - tx * e1z;
+  const float qz = tx * e1y - ty * e1x;
+  const float v = (r.dx * qx + r.dy * qy + r.dz * qz) * inv;
+  if (v < 0.0f || u + v > 1.0f) return false;
+  const float t = (e2x * qx + e2y * qy + e2z * qz) * inv;
+  if (t <= r.tmin || t >= closest) return false;
+  c.t = t;
+  c.e = 0.0f;
+  c.u = u;
+  c.v = v;
+  return true;
+}
+
+__device__ __forceinline__ bool sphere_fast(const RayF& r, float4 c4, float rad, float closest, Cand& c) {
+  const float lx = r.ox - c4.x, ly = r.oy - c4.y, lz = r.oz - c4.z;
+  const float a = r.dx * r.dx + r.dy * r.dy + r.dz * r.dz;
+  const float hb = lx * r.dx + ly * r.dy + lz * r.dz;
+  const float disc = hb * hb - a * (lx * lx + ly * ly + lz * lz - rad * rad);
+  if (disc < 0.0f) return false;
+  const float s = sqrtf(disc);
+  float t = (-hb - s) / a;
+  if (t <= r.tmin || t >= closest) {
+    t = (-hb + s) / a;
+    if (t <= r.tmin || t >= closest) return false;
+  }
+  c.t = t;
+  c.e = 0.0f;
+  c.u = c.v = 0.0f;
+  return true;
+}
+
+// Tests one primitive of a leaf (intersect.ts:155-193).
+// EXACT: a candidate replaces the closest hit when it is nearer by more than
+// both error bounds; when the two distances overlap within their bounds and
+// the bounds are small (a tie within 1e-5), the float32 order decides;
+// otherwise both distances are recomputed in float64 and compared exactly
+// like the reference. Otherwise: plain float32 tests and comparisons.
 // any: returns true for any candidate (occlusion).
+template <bool EXACT>
 __device__ __forceinline__ bool test_prim(const SceneDev& s, const RayF& r, uint32_t p, HitF& h, bool any,
                                           uint32_t& fallbacks) {
   const float4* q = s.prims + (size_t)p * 4;
   const float4 a4 = __ldg(q);
   const float4 b4 = __ldg(q + 1);
   Cand c;
+  if constexpr (!EXACT) {
+    const bool hit = a4.w == 0.0f ? sphere_fast(r, a4, b4.x, h.t, c) : tri_fast(r, a4, b4, __ldg(q + 2), h.t, c);
+    if (!hit) return false;
+    h.prim = (int32_t)p;
+    h.t = c.t;
+    h.u = c.u;
+    h.v = c.v;
+    return any;
+  }
   const bool cand = a4.w == 0.0f ? sphere_candidate(r, a4, b4.x, c, fallbacks)
                                  : tri_candidate(r, a4, b4, __ldg(q + 2), c, fallbacks);
   if (!cand) return false;
@@ -335,11 +393,12 @@ __device__ __forceinline__ bool test_prim(const SceneDev& s, const RayF& r, uint
 }
 
 // All primitives of a leaf; returns true at the first candidate when `any`.
+template <bool EXACT>
 __device__ __forceinline__ bool test_leaf(const SceneDev& s, const RayF& r, uint32_t leafword, HitF& h, bool any,
                                           uint32_t& fallbacks) {
   const uint32_t count = leafword & 7u, start = leafword >> 3;
   for (uint32_t p = start; p < start + count; p++)
-    if (test_prim(s, r, p, h, any, fallbacks)) return true;
+    if (test_prim<EXACT>(s, r, p, h, any, fallbacks)) return true;
   return false;
 }
 
@@ -407,9 +466,10 @@ __device__ __forceinline__ void walk_enter(Walk& w, int32_t c) {
 }
 
 // One step; w.ref == kWalkDone when the query is answered.
+template <bool EXACT>
 __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& fallbacks) {
   if (w.ref == kWalkLeaf) {
-    if (test_prim(s, w.r, w.cur, w.h, w.any, fallbacks)) {
+    if (test_prim<EXACT>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
       w.ref = kWalkDone;
       return;
     }
@@ -456,7 +516,7 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
 // answered is refilled as soon as a quarter of the warp is idle, so lanes
 // keep stepping instead of waiting for the warp's slowest ray. All 32 lanes
 // of every warp must call this (the block size is a multiple of 32).
-template <class Begin, class Finish>
+template <bool EXACT, class Begin, class Finish>
 __device__ __forceinline__ void walk_persistent(const SceneDev& s, uint32_t* counter, uint32_t total, Begin begin,
                                                 Finish finish, uint32_t& fallbacks) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -487,17 +547,18 @@ __device__ __forceinline__ void walk_persistent(const SceneDev& s, uint32_t* cou
       }
     }
     if (__all_sync(0xffffffffu, idx < 0) && drained) break;
-    if (w.ref != kWalkDone) walk_step(s, w, fallbacks);
+    if (w.ref != kWalkDone) walk_step<EXACT>(s, w, fallbacks);
   }
 }
 
 // Complete walk of one query in the calling thread (no refill).
+template <bool EXACT>
 __device__ __forceinline__ bool walk_ordered(const SceneDev& s, const RayF& r, HitF& h, bool any,
                                              uint32_t& fallbacks) {
   Walk w;
   w.r = r;
   walk_begin(s, w, any);
-  while (w.ref != kWalkDone) walk_step(s, w, fallbacks);
+  while (w.ref != kWalkDone) walk_step<EXACT>(s, w, fallbacks);
   h = w.h;
   return !w.overflow;
 }
@@ -513,7 +574,7 @@ __device__ __forceinline__ void walk_stackless(const SceneDev& s, const RayF& r,
     const float4 hi = __ldg(s.nodes + (size_t)node * 2 + 1);
     if (box_entry(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, prune_bound(h)) == INFINITY) {
       node = (uint32_t)lo.w;
-    } else if (hi.w >= 0.0f && test_leaf(s, r, (uint32_t)hi.w, h, any, fallbacks) && any) {
+    } else if (hi.w >= 0.0f && test_leaf<true>(s, r, (uint32_t)hi.w, h, any, fallbacks) && any) {
       node = s.node_count;
     } else {
       node++;
