@@ -38,6 +38,7 @@ for _p in (ROOT / "caustic-tracer_gb300", ROOT / "tests"):
 import numpy as np  # noqa: E402
 
 CORNELL = dict(width=512, height=512, spp=16, max_bounces=8, russian_roulette=False, nee=True, seed=1)
+CAUSTIC = dict(width=1920, height=1080, spp=64, max_bounces=12, russian_roulette=True, nee=True, seed=1)
 TRAVERSAL = dict(triangles=1_000_000, rays=16_777_216, scene_seed=2024, ray_seed=77)
 RAY_BYTES, HIT_BYTES, BOX_BYTES, TRI_BYTES, SPHERE_BYTES = 32, 16, 32, 48, 32
 ACCUM_BYTES_PER_SAMPLE = 12
@@ -49,7 +50,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["cornell", "traversal"], default="cornell")
+    ap.add_argument("--workload", choices=["cornell", "traversal", "caustic"], default="cornell")
     ap.add_argument("--small", action="store_true", help="reduced sizes for profiling captures")
     ap.add_argument("--rays", type=int, default=0, help="traversal: trace only this many rays (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -161,13 +162,20 @@ def traversal_inputs(rank: int, small: bool, rays: int = 0):
     return packed, rays
 
 
-def cornell_inputs(small: bool):
+def render_inputs(workload: str, small: bool):
+    """Packed scene, camera frame and render options of a render workload."""
     import caustic as ct
 
-    cfg = dict(CORNELL)
-    if small:
-        cfg.update(width=128, height=128, spp=4)
-    scene = ct.cornell_unit_box()
+    if workload == "caustic":
+        cfg = dict(CAUSTIC)
+        if small:
+            cfg.update(width=480, height=270, spp=4)
+        scene = ct.caustic_scene(level=5 if small else 7)
+    else:
+        cfg = dict(CORNELL)
+        if small:
+            cfg.update(width=128, height=128, spp=4)
+        scene = ct.cornell_unit_box()
     packed = ct.pack_scene(scene)
     frame = ct.camera_frame(scene.camera, cfg["width"] / cfg["height"])
     return packed, frame, cfg
@@ -193,7 +201,7 @@ def cpu_reference(workload: str, small: bool, target_s: float = 12.0):
                 "sample": f"first {n} of the {len(rays)} rays, ordered walk (intersectClosest), {threads} threads",
                 "bytes_per_unit": bpr, "counts_per_ray": {"aabb": cnt[0] / n, "tri": cnt[1] / n, "sphere": cnt[2] / n},
                 "seconds": dt}
-    packed, frame, cfg = cornell_inputs(small)
+    packed, frame, cfg = render_inputs(workload, small)
     from caustic import _abi
 
     # Rows of the image at full spp until the sample takes long enough.
@@ -283,7 +291,7 @@ def run_reference(args, rank, world):
 
         desc = f"first {n} of the {len(rays)} rays per step, ordered walk (intersectClosest), {threads} threads"
     else:
-        packed, frame, cfg = cornell_inputs(args.small)
+        packed, frame, cfg = render_inputs(args.workload, args.small)
         w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
         rows = max(1, min(h, int(rec["value"] * 1e6 * 2.0 / (w * spp))))
         opts = _abi.ct_render_options(w, rows, spp, cfg["max_bounces"], int(cfg["russian_roulette"]),
@@ -302,7 +310,7 @@ def run_reference(args, rank, world):
         step()
     dt = time.perf_counter() - t0
     value = units * args.steps / dt / 1e6
-    metric = "Msamples/s" if args.workload == "cornell" else "Mrays/s"
+    metric = "Mrays/s" if args.workload == "traversal" else "Msamples/s"
     rec = {"value": value, "unit": metric, "cores": threads, "kind": "port", "sample": desc}
     line = {
         "impl": "reference", "metric": metric, "value": value, "unit": metric, "n_gpus": args.gpus,
@@ -322,11 +330,19 @@ def workload_config(args):
                 "triangles": 100_000 if args.small else TRAVERSAL["triangles"],
                 "rays": (1 << 20) if args.small else TRAVERSAL["rays"],
                 "l2": "inputs larger than L2 (rays 512 MiB per step)", "parallelism": f"replicas x{args.gpus}"}
-    c = dict(CORNELL)
-    if args.small:
-        c.update(width=128, height=128, spp=4)
-    return {"workload": f"cornell box {c['width']}x{c['height']}, {c['spp']} spp, depth {c['max_bounces']}, NEE on, RR off",
-            **c, "l2": "L2 flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{args.gpus}"}
+    if args.workload == "caustic":
+        c = dict(CAUSTIC)
+        if args.small:
+            c.update(width=480, height=270, spp=4)
+        name = (f"caustic scene (icosphere level {5 if args.small else 7} glass blob, 64 spheres, checker ground, "
+                f"sphere light) {c['width']}x{c['height']}, {c['spp']} spp, depth {c['max_bounces']}, NEE on, RR after bounce 3")
+    else:
+        c = dict(CORNELL)
+        if args.small:
+            c.update(width=128, height=128, spp=4)
+        name = f"cornell box {c['width']}x{c['height']}, {c['spp']} spp, depth {c['max_bounces']}, NEE on, RR off"
+    return {"workload": name, **c, "l2": "L2 flushed between timed steps (256 MiB write)",
+            "parallelism": f"replicas x{args.gpus}"}
 
 
 def run_gpu(args, rank, world):
@@ -356,7 +372,7 @@ def run_gpu(args, rank, world):
 
         units_per_step, metric, launches_per_step = n, "Mrays/s", 1
     else:
-        packed, frame, cfg = cornell_inputs(args.small)
+        packed, frame, cfg = render_inputs(args.workload, args.small)
         dev = ct.DeviceScene(packed)
         w, h = cfg["width"], cfg["height"]
         d_out = torch.empty(w * h * 3, dtype=torch.float32, device=device)
@@ -384,7 +400,7 @@ def run_gpu(args, rank, world):
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(torch.cuda.current_device()) as clocks:
         for k in range(args.steps):
-            if args.workload == "cornell":
+            if args.workload != "traversal":
                 flush.fill_(k & 0xFF)  # L2 flush outside the timed events
             starts[k].record(stream)
             step()
@@ -475,15 +491,20 @@ def e2e(args, ct, lib, packed, dev, rank, world, device):
         prim_pin = torch.empty(n, dtype=torch.int32).pin_memory()
         t_pin = torch.empty(n, dtype=torch.float32).pin_memory()
         stats = _abi.ct_stats()
+        parts = {"upload_ms": 0.0, "kernels_ms": 0.0, "wall_ms": 0.0}
 
         def call():
+            t0 = time.perf_counter()
             _native.check(lib.ct_trace_closest(dev.handle, C.c_void_p(rays_pin.data_ptr()), n,
                                                C.c_void_p(prim_pin.data_ptr()), C.c_void_p(t_pin.data_ptr()),
                                                None, None, C.byref(stats)))
+            parts["wall_ms"] += (time.perf_counter() - t0) * 1e3
+            parts["upload_ms"] += stats.total_ms - stats.kernel_ms
+            parts["kernels_ms"] += stats.kernel_ms
 
         h2d, d2h, units, metric = n * 32, n * 8, n, "Mrays/s"
     else:
-        _, frame, cfg = cornell_inputs(args.small)
+        _, frame, cfg = render_inputs(args.workload, args.small)
         w, h = cfg["width"], cfg["height"]
         out = torch.empty(w * h * 3, dtype=torch.float32).pin_memory()
         ropts = ct.RenderOptions(max_bounces=cfg["max_bounces"], russian_roulette=cfg["russian_roulette"],
@@ -492,26 +513,38 @@ def e2e(args, ct, lib, packed, dev, rank, world, device):
         fs = frame.struct()
         view = packed.view()
 
+        parts = {"scene_create_ms": 0.0, "render_and_copy_ms": 0.0, "scene_destroy_ms": 0.0}
+
         def call():
             handle = C.c_void_p()
+            t0 = time.perf_counter()
             _native.check(lib.ct_scene_create(C.byref(view), C.byref(handle)))
+            t1 = time.perf_counter()
             try:
                 _native.check(lib.ct_render_image(handle, C.byref(fs), C.byref(ropts),
                                                   C.c_void_p(out.data_ptr()), None))
             finally:
+                t2 = time.perf_counter()
                 lib.ct_scene_destroy(handle)
+                t3 = time.perf_counter()
+            parts["scene_create_ms"] += (t1 - t0) * 1e3
+            parts["render_and_copy_ms"] += (t2 - t1) * 1e3
+            parts["scene_destroy_ms"] += (t3 - t2) * 1e3
 
         h2d = packed.prims.nbytes + packed.nodes.nbytes + packed.mats.nbytes + packed.lights.nbytes + \
             packed.prim_object.nbytes
         d2h, units, metric = w * h * 12, w * h * cfg["spp"], "Msamples/s"
     call()
+    for k in parts:
+        parts[k] = 0.0
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(steps):
         call()
     dt = max_over_ranks(time.perf_counter() - t0, world, device)
     return {"value": units * steps * world / dt / 1e6, "unit": metric, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "steps": steps}
+            "d2h_bytes_per_step": int(d2h), "steps": steps,
+            "breakdown_ms_per_step": {k: v / steps for k, v in parts.items()}}
 
 
 def main():

@@ -394,6 +394,14 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   // fallbacks, [2B+8, 3B+10) work counters of the persistent trace launches.
   const size_t counter_words = 3 * (size_t)B + 12;
   const size_t bytes = 10 * q_bytes + cap * 8 + counter_words * 4 + 16 * 256;
+  if (s->paths.buf.bytes < bytes) {
+    DeviceBuffer cached;
+    if (path_cache_take(s->device, bytes, cached)) {
+      s->paths.buf.release(&s->device_bytes);
+      s->paths.buf = cached;
+      s->device_bytes += cached.bytes;
+    }
+  }
   ct_status st = s->paths.buf.reserve(bytes, &s->device_bytes);
   if (st != CT_OK) return st;
   char* base = s->paths.buf.as<char>();

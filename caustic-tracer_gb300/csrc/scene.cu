@@ -47,6 +47,41 @@ void DeviceBuffer::release(size_t* total_bytes) {
 }
 
 namespace {
+std::mutex g_cache_mu;
+constexpr int kCacheDevices = 64;
+DeviceBuffer g_path_cache[kCacheDevices];
+}  // namespace
+
+void path_cache_put(int device, DeviceBuffer& b) {
+  if (!b.ptr) return;
+  std::lock_guard<std::mutex> guard(g_cache_mu);
+  if (device < 0 || device >= kCacheDevices) {
+    b.release(nullptr);
+    return;
+  }
+  DeviceBuffer& slot = g_path_cache[device];
+  if (slot.bytes >= b.bytes) {
+    b.release(nullptr);
+  } else {
+    slot.release(nullptr);
+    slot = b;
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+}
+
+bool path_cache_take(int device, size_t want, DeviceBuffer& out) {
+  std::lock_guard<std::mutex> guard(g_cache_mu);
+  if (device < 0 || device >= kCacheDevices) return false;
+  DeviceBuffer& slot = g_path_cache[device];
+  if (!slot.ptr || slot.bytes < want) return false;
+  out = slot;
+  slot.ptr = nullptr;
+  slot.bytes = 0;
+  return true;
+}
+
+namespace {
 
 bool is_index(float f, uint32_t limit) {
   return f >= 0.0f && f < (float)limit && std::floor(f) == f;
@@ -165,8 +200,9 @@ void destroy(ct_scene* s) {
   cudaGetDevice(&prev);
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
+  path_cache_put(s->device, s->paths.buf);
   for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->pairs, &s->mats, &s->lights, &s->prim_object, &s->io,
-                          &s->counters, &s->paths.buf})
+                          &s->counters})
     b->release(&s->device_bytes);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);

@@ -39,6 +39,13 @@ struct PathState {
   uint64_t capacity = 0;     // paths the buffer holds
 };
 
+// Path-state buffers outlive their scenes: ct_scene_destroy hands the buffer
+// to a per-device cache (the largest one is kept) and the next scene on that
+// device adopts it, so a create/render/destroy cycle does not allocate and
+// free hundreds of megabytes each time.
+void path_cache_put(int device, DeviceBuffer& b);
+bool path_cache_take(int device, size_t want, DeviceBuffer& out);
+
 }  // namespace ct
 
 struct ct_scene {

@@ -32,14 +32,14 @@ __global__ void __launch_bounds__(128, 8) k_trace(ctk::SceneDev s, const float4*
     r = ctk::RayF{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, 0.0f, 0.0f, 0.0f};
     ctk::finish_ray(r);
   };
-  // A hit whose float32 distance is looser than ~3 ulp is stored with a
+  // A hit whose float32 distance bound exceeds kReportRel is stored with a
   // negative t; k_refine replaces it with the reference's float64 value.
   auto store = [&](uint32_t i, const ctk::RayF& r, ctk::HitF& h) {
     if (ANY) {
       blocked[i] = h.prim >= 0 ? 1 : 0;
     } else {
       prim[i] = h.prim;
-      t_out[i] = h.prim < 0 ? INFINITY : (h.err > 2e-7f * h.t ? -h.t : h.t);
+      t_out[i] = h.prim < 0 ? INFINITY : (h.err > ctk::kReportRel * h.t ? -h.t : h.t);
       if (u_out) u_out[i] = h.prim >= 0 ? h.u : 0.0f;
       if (v_out) v_out[i] = h.prim >= 0 ? h.v : 0.0f;
     }

@@ -262,8 +262,8 @@ static __device__ __noinline__ double exact_t(const SceneDev& s, const RayF& r, 
   return tri_exact(r, a4, b4, __ldg(q + 2), (double)r.tmin, (double)r.tmax, &t, &u, &v) ? t : -1.0;
 }
 
-// Replaces a closest hit whose float32 distance is looser than ~3 ulp by the
-// reference's float64 t (and barycentrics), once per ray after the walk.
+// Replaces a closest hit's float32 distance by the reference's float64 t
+// (and barycentrics), once per ray after the walk.
 static __device__ __noinline__ void refine_hit(const SceneDev& s, const RayF& r, HitF& h) {
   const float4* q = s.prims + (size_t)h.prim * 4;
   const float4 a4 = __ldg(q), b4 = __ldg(q + 1);
@@ -281,9 +281,9 @@ static __device__ __noinline__ void refine_hit(const SceneDev& s, const RayF& r,
   h.err = rounding_err(h.t);
 }
 
-__device__ __forceinline__ void finish_hit(const SceneDev& s, const RayF& r, HitF& h) {
-  if (h.prim >= 0 && h.err > 2e-7f * h.t) refine_hit(s, r, h);
-}
+// A reported float32 distance whose bound exceeds this (relative) is
+// replaced by the reference's float64 value before it is returned.
+constexpr float kReportRel = 1e-6f;
 
 // Plain float32 forms of the reference's tests (same decisions, float32
 // rounding), for the path integrator whose parity is statistical. The

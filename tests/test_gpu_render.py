@@ -79,14 +79,16 @@ def test_furnace_roulette(furnace):  # furnace.test.ts:65-81
     assert abs(img.mean() - 5) / 5 < 0.03
 
 
-@pytest.mark.parametrize("scene_name,w,h,spp,rr", [("cornell", 96, 64, 16, True), ("unit", 64, 64, 16, False)])
-def test_three_sigma_agreement(oracle, native_lib, scene_name, w, h, spp, rr):
-    sc = ct.CORNELL_BOX if scene_name == "cornell" else ct.cornell_unit_box()
+@pytest.mark.parametrize("scene_name,w,h,spp,rr,bounces", [("cornell", 96, 64, 16, True, 8),
+                                                            ("unit", 64, 64, 16, False, 8),
+                                                            ("caustic", 96, 54, 16, True, 12)])
+def test_three_sigma_agreement(oracle, native_lib, scene_name, w, h, spp, rr, bounces):
+    sc = {"cornell": ct.CORNELL_BOX, "unit": ct.cornell_unit_box()}.get(scene_name) or ct.caustic_scene(level=4)
     packed = ct.pack_scene(sc)
     frame = ct.camera_frame(sc.camera, w / h)
     with ct.DeviceScene(packed) as dev:
-        gpu = gpu_sums(dev, frame, w, h, spp, 1, 8, rr, True)
-    ora = oracle_sums(oracle, packed, frame, w, h, spp, 1, 8, rr, True)
+        gpu = gpu_sums(dev, frame, w, h, spp, 1, bounces, rr, True)
+    ora = oracle_sums(oracle, packed, frame, w, h, spp, 1, bounces, rr, True)
     frac_bad, gm, om = three_sigma(gpu, ora, spp)
     assert frac_bad <= 0.01, f"{frac_bad:.4f} of pixel channels outside 3 standard errors"
     assert abs(gm.mean() / om.mean() - 1) < 0.01
