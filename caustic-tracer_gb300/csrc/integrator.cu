@@ -34,6 +34,7 @@ constexpr int kBlock = 128;
 constexpr int kWarps = kBlock / 32;
 constexpr uint64_t kMaxWavePaths = 8ull << 20;  // paths in flight per wave
 constexpr uint32_t kPersistentDepth = 16;      // tree depth above which traces refill lanes
+constexpr uint32_t kSkipMaxNodes = 31;         // trees this small use the stackless skip-link walk
 
 // Path state of one queue slot (3 x 16 bytes, read and written coalesced):
 //   a = origin.xyz, rng state      b = dir.xyz, pdf (< 0: last bounce specular)
@@ -118,25 +119,33 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
 }
 
 // Closest hits of the bounce-b path queue plus the shadow rays of bounce b-1.
-// PERSISTENT: lanes refill from a work counter as their walks finish (pays
-// off for deep trees); otherwise one walk per thread in a grid-stride loop
-// (cheaper for shallow trees, where walks are short and even).
-template <bool PERSISTENT>
+// Walk forms (chosen per scene by the host):
+//   kWalkThread     ordered walk, one per thread in a grid-stride loop;
+//   kWalkPersistent ordered walk, lanes refill from a work counter as their
+//                   walks finish (pays off for deep trees);
+//   kWalkSkip       the reference's stackless skip-link walk (no stack; all
+//                   lanes visit nodes in the same order; for small trees).
+enum WalkForm : int { kWalkThread = 0, kWalkPersistent = 1, kWalkSkip = 2 };
+
+template <int FORM>
 __global__ void __launch_bounds__(kBlock, 8) k_trace(WaveArgs a, int32_t bounce) {
   const uint32_t n_ext = bounce <= a.max_bounces ? a.counts[bounce] : 0u;
   const uint32_t n_sh = bounce > 0 ? a.counts[a.max_bounces + 2 + bounce - 1] : 0u;
   uint32_t fallbacks = 0;
   // Query i < n_ext: closest hit of path slot i; otherwise shadow ray i - n_ext.
-  auto begin = [&](uint32_t i, ctk::Walk& w) {
+  auto load = [&](uint32_t i, ctk::RayF& r) {
     if (i < n_ext) {
       const float4 ra = a.cur.a[i], rb = a.cur.b[i];
-      w.r = ctk::RayF{ra.x, ra.y, ra.z, rb.x, rb.y, rb.z, ctk::kTMin, INFINITY, 0.0f, 0.0f, 0.0f};
+      r = ctk::RayF{ra.x, ra.y, ra.z, rb.x, rb.y, rb.z, ctk::kTMin, INFINITY, 0.0f, 0.0f, 0.0f};
     } else {
       const uint32_t j = i - n_ext;
       const float4 sa = a.shadow.a[j], sb = a.shadow.b[j];
-      w.r = ctk::RayF{sa.x, sa.y, sa.z, sb.x, sb.y, sb.z, ctk::kTMin, sa.w, 0.0f, 0.0f, 0.0f};
+      r = ctk::RayF{sa.x, sa.y, sa.z, sb.x, sb.y, sb.z, ctk::kTMin, sa.w, 0.0f, 0.0f, 0.0f};
     }
-    ctk::finish_ray(w.r);
+    ctk::finish_ray(r);
+  };
+  auto begin = [&](uint32_t i, ctk::Walk& w) {
+    load(i, w.r);
     ctk::walk_begin(a.scene, w, i >= n_ext);
   };
   auto finish = [&](uint32_t i, ctk::Walk& w) {
@@ -154,15 +163,21 @@ __global__ void __launch_bounds__(kBlock, 8) k_trace(WaveArgs a, int32_t bounce)
       *L = l;
     }
   };
-  if constexpr (PERSISTENT) {
+  if constexpr (FORM == kWalkPersistent) {
     ctk::walk_persistent<false>(a.scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh, begin, finish,
-                         fallbacks);
+                                fallbacks);
   } else {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_ext + n_sh; i += stride) {
       ctk::Walk w;
-      begin(i, w);
-      while (w.ref != ctk::kWalkDone) ctk::walk_step<false>(a.scene, w, fallbacks);
+      if constexpr (FORM == kWalkSkip) {
+        load(i, w.r);
+        w.h = ctk::HitF{-1, w.r.tmax, 0.0f, 0.0f, 0.0f};
+        ctk::walk_stackless<false>(a.scene, w.r, w.h, i >= n_ext, fallbacks);
+      } else {
+        begin(i, w);
+        while (w.ref != ctk::kWalkDone) ctk::walk_step<false>(a.scene, w, fallbacks);
+      }
       finish(i, w);
     }
   }
@@ -339,20 +354,44 @@ int persistent_grid(K kernel) {
 }
 
 struct Grids {
-  int gen = 0, trace = 0, trace_persistent = 0, shade = 0, acc = 0;
+  int gen = 0, trace[3] = {0, 0, 0}, shade = 0, acc = 0;
 };
 
 const Grids& grids() {
   static Grids g = [] {
     Grids r;
     r.gen = persistent_grid(k_generate);
-    r.trace = persistent_grid(k_trace<false>);
-    r.trace_persistent = persistent_grid(k_trace<true>);
+    r.trace[kWalkThread] = persistent_grid(k_trace<kWalkThread>);
+    r.trace[kWalkPersistent] = persistent_grid(k_trace<kWalkPersistent>);
+    r.trace[kWalkSkip] = persistent_grid(k_trace<kWalkSkip>);
     r.shade = persistent_grid(k_shade);
     r.acc = persistent_grid(k_accumulate);
     return r;
   }();
   return g;
+}
+
+// Walk form of a scene's trace launches: the scene's CT_OPT_WALK when set,
+// else by tree size and depth.
+int walk_form(const ct_scene* s) {
+  if (s->opt_walk >= 0) return s->opt_walk;
+  if (s->node_count <= kSkipMaxNodes) return kWalkSkip;
+  return s->depth > kPersistentDepth ? kWalkPersistent : kWalkThread;
+}
+
+void launch_trace(int form, const WaveArgs& w, int32_t bounce, cudaStream_t stream) {
+  const Grids& g = grids();
+  switch (form) {
+    case kWalkPersistent:
+      k_trace<kWalkPersistent><<<g.trace[kWalkPersistent], kBlock, 0, stream>>>(w, bounce);
+      break;
+    case kWalkSkip:
+      k_trace<kWalkSkip><<<g.trace[kWalkSkip], kBlock, 0, stream>>>(w, bounce);
+      break;
+    default:
+      k_trace<kWalkThread><<<g.trace[kWalkThread], kBlock, 0, stream>>>(w, bounce);
+      break;
+  }
 }
 
 ctk::FrameF to_frame(const ct_camera_frame& f) {
@@ -384,7 +423,8 @@ ct_status check_options(const ct_camera_frame* frame, int32_t width, int32_t hei
 ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, uint32_t height, uint32_t first,
                      uint32_t passes, const ct_trace_options& o, float* accum, float* sumsq, cudaStream_t stream) {
   const uint64_t pixels = (uint64_t)width * height;
-  const uint64_t per_wave = std::max<uint64_t>(1, std::min<uint64_t>(passes, kMaxWavePaths / pixels));
+  const uint64_t wave_paths = s->opt_wave_paths > 0 ? (uint64_t)s->opt_wave_paths : kMaxWavePaths;
+  const uint64_t per_wave = std::max<uint64_t>(1, std::min<uint64_t>(passes, wave_paths / pixels));
   const uint64_t cap = per_wave * pixels;
   const int32_t B = o.max_bounces;
   // Layout of the path buffer: 2 queues + shadow queue (3 float4 each per
@@ -433,14 +473,10 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   }
   a.sky_strength = (float)s->sky.strength;
   const Grids& g = grids();
-  // Deep trees make walk lengths uneven: refill lanes from a work counter.
-  const bool persistent = s->depth > kPersistentDepth;
+  const int form = walk_form(s);
   auto trace = [&](const WaveArgs& w, int32_t b) {
     ProfScope ps("trace", stream);
-    if (persistent)
-      k_trace<true><<<g.trace_persistent, kBlock, 0, stream>>>(w, b);
-    else
-      k_trace<false><<<g.trace, kBlock, 0, stream>>>(w, b);
+    launch_trace(form, w, b, stream);
   };
   for (uint64_t done = 0; done < passes; done += per_wave) {
     const uint32_t p = (uint32_t)std::min<uint64_t>(per_wave, passes - done);
@@ -684,14 +720,11 @@ ct_status ct_accumulate_pass_noalloc(ct_scene* scene, const ct_camera_frame* fra
   // The array keeps the previous call's contents: the counters must start at zero.
   CT_CUDA(cudaMemsetAsync(a.counts, 0, counter_words * 4, s));
   const Grids& g = grids();
-  const bool persistent = scene->depth > kPersistentDepth;
+  const int form = walk_form(scene);
   k_generate<<<g.gen, kBlock, 0, s>>>(a);
   WaveArgs w = a;
   for (int32_t b = 0; b <= B + 1; b++) {
-    if (persistent)
-      k_trace<true><<<g.trace_persistent, kBlock, 0, s>>>(w, b);
-    else
-      k_trace<false><<<g.trace, kBlock, 0, s>>>(w, b);
+    launch_trace(form, w, b, s);
     if (b > B) break;
     k_shade<<<g.shade, kBlock, 0, s>>>(w, b);
     std::swap(w.cur, w.next);

@@ -321,4 +321,24 @@ void ct_scene_destroy(ct_scene* scene) { ct::destroy(scene); }
 
 uint64_t ct_scene_device_bytes(const ct_scene* scene) { return scene ? scene->device_bytes : 0; }
 
+ct_status ct_scene_set_option(ct_scene* scene, int32_t option, int64_t value) {
+  ct::clear_error();
+  CT_CHECK_ARG(scene != nullptr, "scene is NULL");
+  std::lock_guard<std::mutex> guard(scene->lock);
+  switch (option) {
+    case CT_OPT_WALK:
+      CT_CHECK_ARG(value >= -1 && value <= 2, "CT_OPT_WALK %lld outside [-1, 2]", (long long)value);
+      if (value == 0 || value == 1)
+        CT_CHECK_ARG(scene->depth <= ctk::kStackSize, "tree depth %u exceeds the ordered walk's stack", scene->depth);
+      scene->opt_walk = (int32_t)value;
+      return CT_OK;
+    case CT_OPT_WAVE_PATHS:
+      CT_CHECK_ARG(value >= 0 && value <= (1ll << 30), "CT_OPT_WAVE_PATHS %lld outside [0, 2^30]", (long long)value);
+      scene->opt_wave_paths = value;
+      return CT_OK;
+    default:
+      return ct::fail(CT_ERR_INVALID_ARGUMENT, "unknown scene option %d", option);
+  }
+}
+
 }  // extern "C"

@@ -66,6 +66,11 @@ struct ct_scene {
   ct::PathState paths;
   size_t device_bytes = 0;
 
+  // Tuning options (ct_scene_set_option): integrator walk form (-1 = chosen
+  // from the tree) and paths per wave (0 = library default).
+  int32_t opt_walk = -1;
+  int64_t opt_wave_paths = 0;
+
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
 };
 

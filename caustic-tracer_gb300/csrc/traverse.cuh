@@ -565,7 +565,9 @@ __device__ __forceinline__ bool walk_ordered(const SceneDev& s, const RayF& r, H
 
 // Stackless skip-link walk over the reference node array, the literal
 // mirror of intersectClosestStackless (intersect.ts:290-365) and occluded
-// (intersect.ts:368-420).
+// (intersect.ts:368-420). Needs no stack; every lane visits nodes in the
+// same increasing order, which keeps small trees in lockstep.
+template <bool EXACT = true>
 __device__ __forceinline__ void walk_stackless(const SceneDev& s, const RayF& r, HitF& h, bool any,
                                                uint32_t& fallbacks) {
   uint32_t node = 0;
@@ -574,7 +576,7 @@ __device__ __forceinline__ void walk_stackless(const SceneDev& s, const RayF& r,
     const float4 hi = __ldg(s.nodes + (size_t)node * 2 + 1);
     if (box_entry(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, prune_bound(h)) == INFINITY) {
       node = (uint32_t)lo.w;
-    } else if (hi.w >= 0.0f && test_leaf<true>(s, r, (uint32_t)hi.w, h, any, fallbacks) && any) {
+    } else if (hi.w >= 0.0f && test_leaf<EXACT>(s, r, (uint32_t)hi.w, h, any, fallbacks) && any) {
       node = s.node_count;
     } else {
       node++;

@@ -196,6 +196,16 @@ void ct_scene_destroy(ct_scene* scene);
 /* Device bytes held by the scene (for admission budgets). */
 uint64_t ct_scene_device_bytes(const ct_scene* scene);
 
+/* Per-scene tuning knobs, set by callers or an autotuner. No counterpart in
+ * the reference (its CPU loop has nothing to tune).
+ *   CT_OPT_WALK        integrator trace walk: -1 chosen from the tree (default),
+ *                      0 ordered walk per thread, 1 ordered walk with persistent
+ *                      lane refill, 2 stackless skip-link walk (intersect.ts:290)
+ *   CT_OPT_WAVE_PATHS  paths in flight per wave (0 = library default, 8 Mi)    */
+#define CT_OPT_WALK 1
+#define CT_OPT_WAVE_PATHS 2
+ct_status ct_scene_set_option(ct_scene* scene, int32_t option, int64_t value);
+
 /* ---- ray queries --------------------------------------------------------
  * intersectClosest (intersect.ts:202-282) over a batch of rays. rays holds
  * CT_RAY_FLOATS floats per ray. prim receives the packed primitive index or
