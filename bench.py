@@ -50,7 +50,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["cornell", "traversal", "caustic"], default="cornell")
+    ap.add_argument("--workload", choices=["cornell", "traversal", "caustic", "batched"], default="cornell")
+    ap.add_argument("--jobs", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--small", action="store_true", help="reduced sizes for profiling captures")
     ap.add_argument("--rays", type=int, default=0, help="traversal: trace only this many rays (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -547,6 +548,101 @@ def e2e(args, ct, lib, packed, dev, rank, world, device):
             "breakdown_ms_per_step": {k: v / steps for k, v in parts.items()}}
 
 
+def batched_inputs(count: int, small: bool):
+    """Packed scenes and render sizes of the batched workload (packing runs in parallel threads)."""
+    import concurrent.futures as cf
+
+    import caustic as ct
+
+    spec = ct.batch_workload(count, max_tris=20_000 if small else 200_000)
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        packed = list(ex.map(lambda s: ct.pack_scene(s[0]), spec))
+    return [(p, ct.camera_frame(s.camera, w / h), w, h) for p, (s, w, h) in zip(packed, spec)]
+
+
+def run_batched(args, rank, world):
+    """Batched form: all jobs in one graph launch vs the same jobs as sequential plain renders."""
+    import torch
+
+    import caustic as ct
+    from caustic import _native
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    device = torch.device("cuda", torch.cuda.current_device())
+    spp = 4 if args.small else 16
+    opts = ct.TraceOptions(max_bounces=8, russian_roulette=True, nee=True)
+    inputs = batched_inputs(args.jobs, args.small)
+    scenes = [ct.DeviceScene(p) for p, _, _, _ in inputs]
+    jobs = [ct.Job(d, f, w, h, spp, seed=1 + i + 1000 * rank) for i, (d, (_, f, w, h)) in enumerate(zip(scenes, inputs))]
+    samples = sum(j.width * j.height * spp for j in jobs)
+    stream = torch.cuda.Stream()
+    br = ct.BatchRenderer(jobs, opts)
+    lib = _native.lib()
+    outs = [torch.empty(j.width * j.height * 3, device=device) for j in jobs]
+    ropts = [ct.RenderOptions(max_bounces=8, russian_roulette=True, nee=True, width=j.width, height=j.height,
+                              spp=spp, seed=j.seed).struct() for j in jobs]
+    fstructs = [j.frame.struct() for j in jobs]
+
+    def batched_step():
+        br.run(stream)
+
+    def plain_step():
+        for j, o, f, out in zip(jobs, ropts, fstructs, outs):
+            _native.check(lib.ct_render_image_device(j.scene.handle, C.byref(f), C.byref(o), _native.ptr(out),
+                                                     C.c_void_p(stream.cuda_stream)))
+
+    def timed(step, steps):
+        with torch.cuda.stream(stream):
+            for _ in range(max(3, args.warmup)):
+                step()
+        torch.cuda.synchronize()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1) / 1e3, world, device)
+
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        t_batch = timed(batched_step, args.steps)
+    t_plain = timed(plain_step, max(1, args.steps // 2))
+    plain_rate = samples * max(1, args.steps // 2) * world / t_plain / 1e6
+    value = samples * args.steps * world / t_batch / 1e6
+    # end to end: graph launch + copy of every job's sums to the host
+    t0 = time.perf_counter()
+    for _ in range(2):
+        br.run(stream)
+        torch.cuda.synchronize()
+        _ = [a.cpu() for a in br.accums]
+    e2e_rate = samples * 2 * world / (time.perf_counter() - t0) / 1e6
+    info = br.info()
+    line = {
+        "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_batch * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, Rng of the reference)",
+        "config": {"workload": f"batched: {len(jobs)} scenes (soups of 2k-{20_000 if args.small else 200_000} "
+                               f"triangles, 0-32 spheres, quad light), sizes 64-512 squared, {spp} spp, depth 8, "
+                               f"one CUDA graph per run",
+                   "jobs": len(jobs), "triangles": int(sum(p.prim_count for p, _, _, _ in inputs)),
+                   "samples_per_step": samples, "waves": info["waves"], "graph_nodes": info["graph_nodes"],
+                   "walk": info["walk"], "parallelism": f"replicas x{args.gpus}"},
+        "plain_sequential": {"value": plain_rate, "unit": "Msamples/s",
+                             "what": "the same jobs as consecutive ct_render_image_device calls"},
+        "speedup_vs_plain": value / plain_rate,
+        "clocks": clocks.summary(),
+        "e2e": {"value": e2e_rate, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(sum(j.width * j.height * 12 for j in jobs)),
+                "what": "graph launch + device-to-host copy of all sums; scenes stay resident"},
+    }
+    br.close()
+    for d in scenes:
+        d.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -561,6 +657,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, rank, world)
+        elif args.workload == "batched":
+            run_batched(args, rank, world)
         else:
             run_gpu(args, rank, world)
     finally:

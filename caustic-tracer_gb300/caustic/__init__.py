@@ -11,8 +11,9 @@ from .rng import Rng, pcg_hash, seed_for
 from .scene import (CameraSettings, CheckerTexture, Dielectric, Emissive, Lambertian, Mesh, Metal, Quad,
                     Scene, SceneObject, SkyGradient, SkyNone, Sphere, Triangle, material_emission,
                     primitive_count, quad_triangles, triangle_area, triangle_normal)
-from .scenes import (CORNELL_BOX, caustic_scene, cornell_box, cornell_unit_box, furnace_scene,
-                     random_test_scene, soup_rays, triangle_soup)
+from .scenes import (CORNELL_BOX, batch_scene, batch_workload, caustic_scene, cornell_box, cornell_unit_box,
+                     furnace_scene, random_test_scene, soup_rays, triangle_soup)
+from .batch import BatchRenderer, Job
 from .tonemap import decode_ppm, encode_ppm, tonemap_buffer
 from .tracer import (DEFAULT_TRACE_OPTIONS, T_MIN, DeviceScene, Hits, RenderOptions, TraceOptions,
                      accumulate_pass, intersect_closest, make_rays, occluded, render_image, set_traversal)

@@ -111,6 +111,18 @@ class ct_packed_scene(C.Structure):
     _fields_ = [("view", ct_packed_scene_view), ("order", C.POINTER(C.c_uint32))]
 
 
+class ct_batch_job(C.Structure):
+    _fields_ = [
+        ("scene", C.c_void_p),
+        ("frame", ct_camera_frame),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("first_frame_index", C.c_uint32),
+        ("passes", C.c_int32),
+        ("accum", C.c_void_p),
+    ]
+
+
 class ct_stats(C.Structure):
     _fields_ = [
         ("kernel_ms", C.c_double),
@@ -144,6 +156,13 @@ SIGNATURES = {
     "ct_accumulate_passes_device": (C.c_int, [P, C.POINTER(ct_camera_frame), C.c_int32, C.c_int32, C.c_uint32,
                                               C.c_int32, C.POINTER(ct_trace_options), P, P, P]),
     "ct_render_image_device": (C.c_int, [P, C.POINTER(ct_camera_frame), C.POINTER(ct_render_options), P, P]),
+    "ct_batch_create": (C.c_int, [C.POINTER(ct_batch_job), C.c_uint32, C.POINTER(ct_trace_options), C.c_int64,
+                                  C.c_int32, C.POINTER(P)]),
+    "ct_batch_set_first_frames": (C.c_int, [P, C.POINTER(C.c_uint32)]),
+    "ct_batch_run": (C.c_int, [P, P]),
+    "ct_batch_info": (C.c_int, [P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                C.POINTER(C.c_int32)]),
+    "ct_batch_destroy": (None, [P]),
     "ct_accumulate_pass_noalloc": (C.c_int, [P, C.POINTER(ct_camera_frame), C.c_int32, C.c_int32, C.c_uint32,
                                              C.POINTER(ct_trace_options), P, P]),
     "ct_profile_enable": (None, [C.c_int32]),

@@ -202,6 +202,39 @@ def _random_material(rng: Rng):
     return Dielectric(1.5)
 
 
+def batch_scene(seed: int, triangles: int, spheres: int) -> Scene:
+    """One scene of the batched workload: a triangle soup as in triangle_soup()
+    (Lambertian, random albedo), `spheres` spheres of radius U(0.02, 0.08)
+    inside the cube with materials drawn as in caustic_scene(), and one
+    0.3 x 0.3 ceiling light quad above the cube with emission 15."""
+    rng = Rng(seed)
+    soup = triangle_soup(triangles, seed=seed * 7 + 1)
+    n = [0]
+    albedo = (rng.range(0.2, 0.9), rng.range(0.2, 0.9), rng.range(0.2, 0.9))
+    objects = [SceneObject("soup", "soup", soup.objects[0].shape, Lambertian(albedo)),
+               _obj("Light", Quad((-0.15, 0.7, -0.15), (0.3, 0, 0), (0, 0, 0.3)), Emissive((1, 1, 1), 15), n)]
+    for i in range(spheres):
+        c = (rng.range(-0.45, 0.45), rng.range(-0.45, 0.45), rng.range(-0.45, 0.45))
+        objects.append(_obj(f"Sphere {i + 1}", Sphere(c, rng.range(0.02, 0.08)), _random_material(rng), n))
+    return Scene(f"batch {seed}", objects, camera_at((0.0, 0.3, 2.0), (0, 0, 0), 45, 0), SkyNone())
+
+
+def batch_workload(count: int = 256, seed: int = 4096, min_tris: int = 2_000, max_tris: int = 200_000,
+                   max_spheres: int = 32, sizes=(64, 128, 256, 512)):
+    """(scene, width, height) for `count` batched-workload scenes: triangle counts
+    log-uniform in [min_tris, max_tris], 0..max_spheres spheres, square images
+    with a side drawn uniformly from `sizes` (all choices from Rng(seed))."""
+    rng = Rng(seed)
+    out = []
+    lo, hi = math.log(min_tris), math.log(max_tris)
+    for i in range(count):
+        tris = int(round(math.exp(rng.range(lo, hi))))
+        spheres = rng.int(max_spheres + 1)
+        side = sizes[rng.int(len(sizes))]
+        out.append((batch_scene(seed + 1 + i, tris, spheres), side, side))
+    return out
+
+
 def caustic_scene(seed: int = 7, level: int = 7) -> Scene:
     """Caustic workload: glass icosphere (level 7 = 327,680 triangles, radius 0.8,
     radial value-noise displacement of amplitude 0.05), 64 spheres of radius

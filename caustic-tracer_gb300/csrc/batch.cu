@@ -1,0 +1,290 @@
+// Batched rendering: many scenes, cameras and image sizes in one graph.
+//
+// A batch is a list of jobs (scene, camera, size, frame indices, passes, sum
+// buffer). Their paths are packed into waves of up to `wave_paths` paths: the
+// planner walks passes in order and appends each job's pass as one segment
+// (split across waves when it does not fit), opening a new wave whenever a
+// job would appear twice in one, so every wave holds at most one pass of any
+// pixel and per-pixel sums stay in pass order. All waves run on the shared
+// wavefront kernels (BATCH = true), each path finding its scene, sky, camera
+// and output through its job record. The full launch sequence of all waves is
+// captured once into a CUDA graph and replayed by every ct_batch_run; the
+// frame indices live in a device table, so progressive passes reuse the same
+// graph (ct_batch_set_first_frames).
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "profile.hpp"
+#include "scene.hpp"
+#include "wavefront.cuh"
+
+struct ct_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;  // used when ct_batch_run gets no stream
+  ct_trace_options opts{};
+  int walk = 0;
+  std::vector<ct_batch_job> jobs;
+  std::vector<ct::SegDev> segs;            // all waves, host copy
+  std::vector<uint32_t> seg_pass;          // pass number of each segment
+  struct Wave {
+    uint32_t seg0, nsegs, paths;
+  };
+  std::vector<Wave> waves;
+  uint64_t max_paths = 0, total_paths = 0;
+  ct::DeviceBuffer d_jobs, d_segs, d_paths;
+  ct::WaveArgs base{};
+  size_t counter_words = 0;
+  bool segs_dirty = true;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  size_t graph_nodes = 0;
+};
+
+namespace ct {
+namespace {
+
+constexpr uint64_t kDefaultWavePaths = 8ull << 20;
+constexpr uint32_t kBatchSkipMaxNodes = 31;
+
+void plan(ct_batch* b, uint64_t cap) {
+  uint32_t max_passes = 0;
+  for (const ct_batch_job& j : b->jobs) max_passes = std::max<uint32_t>(max_passes, (uint32_t)j.passes);
+  std::vector<int64_t> last_wave(b->jobs.size(), -1);
+  auto open = [&]() { b->waves.push_back({(uint32_t)b->segs.size(), 0, 0}); };
+  open();
+  for (uint32_t q = 0; q < max_passes; q++) {
+    for (uint32_t j = 0; j < b->jobs.size(); j++) {
+      const ct_batch_job& job = b->jobs[j];
+      if ((uint32_t)job.passes <= q) continue;
+      const uint32_t pixels = (uint32_t)job.width * (uint32_t)job.height;
+      uint32_t done = 0;
+      while (done < pixels) {
+        ct_batch::Wave* w = &b->waves.back();
+        if (last_wave[j] == (int64_t)b->waves.size() - 1 || w->paths >= cap) {
+          open();
+          w = &b->waves.back();
+        }
+        const uint32_t take = (uint32_t)std::min<uint64_t>(pixels - done, cap - w->paths);
+        b->segs.push_back(SegDev{j, job.first_frame_index + q, done, w->paths});
+        b->seg_pass.push_back(q);
+        w->nsegs++;
+        w->paths += take;
+        done += take;
+        last_wave[j] = (int64_t)b->waves.size() - 1;
+      }
+    }
+  }
+  if (b->waves.back().nsegs == 0) b->waves.pop_back();
+  for (const auto& w : b->waves) {
+    b->max_paths = std::max<uint64_t>(b->max_paths, w.paths);
+    b->total_paths += w.paths;
+  }
+}
+
+// Enqueues every wave of the batch on `s` (captured into the graph).
+ct_status enqueue_all(ct_batch* b, cudaStream_t s) {
+  const Grids<true>& g = grids<true>();
+  const int32_t B = b->opts.max_bounces;
+  for (const auto& wv : b->waves) {
+    WaveArgs a = b->base;
+    a.segs = b->d_segs.as<SegDev>() + wv.seg0;
+    a.nsegs = wv.nsegs;
+    a.paths = wv.paths;
+    CT_CUDA(cudaMemsetAsync(a.counts, 0, b->counter_words * 4, s));
+    k_generate<true><<<g.gen, kBlock, 0, s>>>(a);
+    WaveArgs w = a;
+    for (int32_t bounce = 0; bounce <= B; bounce++) {
+      launch_trace<true>(b->walk, w, bounce, s);
+      k_shade<true><<<g.shade, kBlock, 0, s>>>(w, bounce);
+      std::swap(w.cur, w.next);
+    }
+    launch_trace<true>(b->walk, w, B + 1, s);
+    k_accumulate_batch<<<g.acc, kBlock, 0, s>>>(a);
+  }
+  CT_CUDA(cudaGetLastError());
+  return CT_OK;
+}
+
+void destroy(ct_batch* b) {
+  if (!b) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->d_jobs.release(nullptr);
+  b->d_segs.release(nullptr);
+  b->d_paths.release(nullptr);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  cudaSetDevice(prev);
+  delete b;
+}
+
+ct_status create(const ct_batch_job* jobs, uint32_t count, const ct_trace_options* o, int64_t wave_paths,
+                 int32_t walk, ct_batch** out) {
+  CT_CHECK_ARG(jobs != nullptr && count > 0 && o != nullptr && out != nullptr, "NULL argument or empty batch");
+  CT_CHECK_ARG(walk == -1 || walk == 0 || walk == 2, "batch walk %d must be -1 (auto), 0 or 2", walk);
+  CT_CHECK_ARG(wave_paths >= 0 && wave_paths <= (1ll << 30), "wave_paths %lld outside [0, 2^30]", (long long)wave_paths);
+  const int device = jobs[0].scene ? jobs[0].scene->device : -1;
+  bool all_small = true;
+  for (uint32_t i = 0; i < count; i++) {
+    const ct_batch_job& j = jobs[i];
+    CT_CHECK_ARG(j.scene != nullptr && j.accum != nullptr, "job %u: NULL scene or accum", i);
+    CT_CHECK_ARG(j.scene->device == device, "job %u: scene lives on device %d, job 0 on %d", i, j.scene->device, device);
+    CT_CHECK_ARG(j.passes >= 0, "job %u: passes %d is negative", i, j.passes);
+    if (walk == 0) CT_CHECK_ARG(j.scene->depth <= ctk::kStackSize, "job %u: tree too deep for the ordered walk", i);
+    ct_status st = check_options(&j.frame, j.width, j.height, o->max_bounces);
+    if (st != CT_OK) return fail(st, "job %u: %s", i, last_error());
+    all_small = all_small && j.scene->node_count <= kBatchSkipMaxNodes;
+    if (j.scene->depth > ctk::kStackSize) all_small = true;  // deep trees need the stackless walk
+  }
+  const uint64_t cap = wave_paths > 0 ? (uint64_t)wave_paths : kDefaultWavePaths;
+  ct_batch* b = new (std::nothrow) ct_batch();
+  if (!b) return fail(CT_ERR_OUT_OF_MEMORY, "ct_batch_create: host allocation failed");
+  b->device = device;
+  b->opts = *o;
+  b->walk = walk >= 0 ? walk : (all_small ? kWalkSkip : kWalkThread);
+  b->jobs.assign(jobs, jobs + count);
+  auto bail = [&](ct_status code) {
+    destroy(b);
+    return code;
+  };
+  try {
+    plan(b, cap);
+  } catch (const std::bad_alloc&) {
+    return bail(fail(CT_ERR_OUT_OF_MEMORY, "ct_batch_create: host allocation failed"));
+  }
+  {
+    cudaError_t err = cudaSetDevice(device);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (err != cudaSuccess) {
+      b->stream = nullptr;
+      return bail(fail(CT_ERR_CUDA, "ct_batch_create: %s", cudaGetErrorString(err)));
+    }
+  }
+  std::vector<JobDev> host_jobs(count);
+  for (uint32_t i = 0; i < count; i++) {
+    const ct_batch_job& j = jobs[i];
+    host_jobs[i].scene = j.scene->dev;
+    host_jobs[i].sky = to_sky(j.scene->sky);
+    host_jobs[i].frame = to_frame(j.frame);
+    host_jobs[i].width = (uint32_t)j.width;
+    host_jobs[i].height = (uint32_t)j.height;
+    host_jobs[i].accum = j.accum;
+  }
+  const uint64_t cap_paths = std::max<uint64_t>(1, b->max_paths);
+  const size_t q = cap_paths * sizeof(float4), w4 = cap_paths * 4;
+  b->counter_words = wave_counter_words(o->max_bounces);
+  const size_t bytes = 10 * q + 6 * w4 + b->counter_words * 4 + 20 * 256;
+  ct_status st;
+  if ((st = b->d_jobs.reserve(host_jobs.size() * sizeof(JobDev), nullptr)) != CT_OK ||
+      (st = b->d_segs.reserve(std::max<size_t>(1, b->segs.size()) * sizeof(SegDev), nullptr)) != CT_OK ||
+      (st = b->d_paths.reserve(bytes, nullptr)) != CT_OK)
+    return bail(st);
+  {
+    cudaError_t err = cudaMemcpyAsync(b->d_jobs.ptr, host_jobs.data(), host_jobs.size() * sizeof(JobDev),
+                                      cudaMemcpyHostToDevice, b->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(b->stream);
+    if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "batch upload: %s", cudaGetErrorString(err)));
+  }
+  char* base = b->d_paths.as<char>();
+  auto take = [&](size_t n) {
+    char* p = base;
+    base += (n + 255) & ~size_t(255);
+    return p;
+  };
+  WaveArgs& a = b->base;
+  a.cur = Queue{(float4*)take(q), (float4*)take(q), (float4*)take(q), (uint32_t*)take(w4)};
+  a.next = Queue{(float4*)take(q), (float4*)take(q), (float4*)take(q), (uint32_t*)take(w4)};
+  a.shadow = ShadowQueue{(float4*)take(q), (float4*)take(q), (float4*)take(q)};
+  a.radiance = (float4*)take(q);
+  a.hit_prim = (int32_t*)take(w4);
+  a.hit_t = (float*)take(w4);
+  a.path_job = (uint32_t*)take(w4);
+  a.path_pixel = (uint32_t*)take(w4);
+  a.counts = (uint32_t*)take(b->counter_words * 4);
+  a.jobs = b->d_jobs.as<JobDev>();
+  a.max_bounces = o->max_bounces;
+  a.rr = o->russian_roulette;
+  a.nee = o->nee;
+  *out = b;
+  return CT_OK;
+}
+
+ct_status run(ct_batch* b, cudaStream_t s) {
+  CT_CUDA(cudaSetDevice(b->device));
+  if (b->segs_dirty && !b->segs.empty()) {
+    CT_CUDA(cudaMemcpyAsync(b->d_segs.ptr, b->segs.data(), b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, s));
+    b->segs_dirty = false;
+  }
+  if (b->waves.empty()) return CT_OK;
+  if (!b->exec) {
+    (void)grids<true>();  // occupancy queries before capture
+    cudaStream_t cap = b->stream;
+    CT_CUDA(cudaStreamSynchronize(s));  // the segment upload above precedes the capture
+    CT_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    ct_status st = enqueue_all(b, cap);
+    cudaGraph_t graph = nullptr;
+    cudaError_t err = cudaStreamEndCapture(cap, &graph);
+    if (st != CT_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return st;
+    }
+    if (err != cudaSuccess) return fail(CT_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(err));
+    b->graph = graph;
+    CT_CUDA(cudaGraphGetNodes(graph, nullptr, &b->graph_nodes));
+    CT_CUDA(cudaGraphInstantiate(&b->exec, graph, 0));
+  }
+  ProfScope ps("batch_graph", s);
+  CT_CUDA(cudaGraphLaunch(b->exec, s));
+  return CT_OK;
+}
+
+}  // namespace
+}  // namespace ct
+
+extern "C" {
+
+ct_status ct_batch_create(const ct_batch_job* jobs, uint32_t count, const ct_trace_options* opts, int64_t wave_paths,
+                          int32_t walk, ct_batch** out) {
+  ct::clear_error();
+  if (out) *out = nullptr;
+  try {
+    return ct::create(jobs, count, opts, wave_paths, walk, out);
+  } catch (const std::bad_alloc&) {
+    return ct::fail(CT_ERR_OUT_OF_MEMORY, "ct_batch_create: host allocation failed");
+  }
+}
+
+ct_status ct_batch_set_first_frames(ct_batch* batch, const uint32_t* first_frame_index) {
+  ct::clear_error();
+  CT_CHECK_ARG(batch != nullptr && first_frame_index != nullptr, "NULL argument");
+  for (size_t i = 0; i < batch->segs.size(); i++)
+    batch->segs[i].frame_index = first_frame_index[batch->segs[i].job] + batch->seg_pass[i];
+  batch->segs_dirty = true;
+  return CT_OK;
+}
+
+ct_status ct_batch_run(ct_batch* batch, void* stream) {
+  ct::clear_error();
+  CT_CHECK_ARG(batch != nullptr, "batch is NULL");
+  return ct::run(batch, stream ? static_cast<cudaStream_t>(stream) : batch->stream);
+}
+
+ct_status ct_batch_info(const ct_batch* batch, uint32_t* waves, uint64_t* paths, uint64_t* graph_nodes,
+                        int32_t* walk) {
+  ct::clear_error();
+  CT_CHECK_ARG(batch != nullptr, "batch is NULL");
+  if (waves) *waves = (uint32_t)batch->waves.size();
+  if (paths) *paths = batch->total_paths;
+  if (graph_nodes) *graph_nodes = batch->graph_nodes;
+  if (walk) *walk = batch->walk;
+  return CT_OK;
+}
+
+void ct_batch_destroy(ct_batch* batch) { ct::destroy(batch); }
+
+}  // extern "C"

@@ -12,6 +12,7 @@ namespace ct {
 // Records `msg` as the calling thread's last error and returns `status`.
 ct_status fail(ct_status status, const char* fmt, ...);
 void clear_error();
+const char* last_error();
 
 }  // namespace ct
 

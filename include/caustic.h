@@ -249,6 +249,39 @@ ct_status ct_accumulate_passes_device(ct_scene* scene, const ct_camera_frame* fr
 ct_status ct_render_image_device(ct_scene* scene, const ct_camera_frame* frame,
                                  const ct_render_options* opts, float* out, void* stream);
 
+/* ---- batched rendering ----------------------------------------------------
+ * Many scenes, cameras and image sizes rendered together. No single
+ * counterpart in the reference: each job is `passes` calls of accumulatePass
+ * (tracer.ts:361-395) with frame indices first_frame_index + k, adding into
+ * the job's device sum buffer `accum` (width*height*3 floats). Results equal
+ * those of the single-scene entry points for the same frame indices.
+ * The paths of all jobs share waves of up to wave_paths paths (0 = 8 Mi);
+ * walk selects the trace walk (-1 auto, 0 ordered, 2 stackless skip-link).
+ * The first ct_batch_run captures the whole launch sequence in a CUDA graph;
+ * later runs replay it. Scenes must outlive the batch and must not be used
+ * by other calls while a run is in flight.                                  */
+typedef struct ct_batch_job {
+  ct_scene* scene;
+  ct_camera_frame frame;
+  int32_t width;
+  int32_t height;
+  uint32_t first_frame_index;
+  int32_t passes;
+  float* accum;
+} ct_batch_job;
+
+typedef struct ct_batch ct_batch;
+
+ct_status ct_batch_create(const ct_batch_job* jobs, uint32_t count, const ct_trace_options* opts,
+                          int64_t wave_paths, int32_t walk, ct_batch** out);
+/* Replaces every job's first frame index (one per job) for the next run. */
+ct_status ct_batch_set_first_frames(ct_batch* batch, const uint32_t* first_frame_index);
+/* Enqueues the batch on `stream` (NULL = the batch's own stream). */
+ct_status ct_batch_run(ct_batch* batch, void* stream);
+ct_status ct_batch_info(const ct_batch* batch, uint32_t* waves, uint64_t* paths, uint64_t* graph_nodes,
+                        int32_t* walk);
+void ct_batch_destroy(ct_batch* batch);
+
 /* ---- accumulatePass without allocation ------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device
  * memory when they render: code recording a CUDA graph (cudaMalloc is not

@@ -1,0 +1,88 @@
+"""Batched rendering (ct_batch_*): every job's image equals the single-scene
+render with the same frame indices, whatever the wave packing, and the
+graph replays accumulate further passes correctly."""
+import numpy as np
+import pytest
+
+import caustic as ct
+
+pytestmark = pytest.mark.gpu
+
+
+def _jobs(scenes, spp=3):
+    jobs = []
+    for i, (sc, w, h) in enumerate(scenes):
+        dev = ct.DeviceScene.from_scene(sc)
+        jobs.append(ct.Job(dev, ct.camera_frame(sc.camera, w / h), w, h, spp, seed=i + 1))
+    return jobs
+
+
+def _single(job, opts, walk):
+    # Same trace walk as the batch: in float32, walks that visit nodes in a
+    # different order can break exact ties (a quad's shared diagonal) the
+    # other way, which changes a path but not the estimator.
+    from caustic import _native
+
+    _native.check(job.scene._lib.ct_scene_set_option(job.scene.handle, 1, walk))
+    return ct.render_image(job.scene, job.frame, ct.RenderOptions(
+        max_bounces=opts.max_bounces, russian_roulette=opts.russian_roulette, nee=opts.nee,
+        width=job.width, height=job.height, spp=job.spp, seed=job.seed))
+
+
+@pytest.fixture(scope="module")
+def scenes(native_lib):
+    out = [(ct.batch_scene(11, 2_000, 3), 48, 48), (ct.batch_scene(12, 20_000, 0), 32, 24),
+           (ct.cornell_unit_box(), 40, 40), (ct.caustic_scene(level=3), 36, 20), (ct.CORNELL_BOX, 24, 16),
+           (ct.batch_scene(13, 5_000, 12), 17, 9)]
+    return out
+
+
+@pytest.mark.parametrize("wave_paths,walk", [(0, -1), (1000, -1), (777, 0), (5000, 2)])
+def test_batch_equals_single_renders(scenes, wave_paths, walk):
+    opts = ct.TraceOptions(max_bounces=8, russian_roulette=True, nee=True)
+    jobs = _jobs(scenes)
+    with ct.BatchRenderer(jobs, opts, wave_paths=wave_paths, walk=walk) as br:
+        br.run()
+        imgs = br.images()
+        info = br.info()
+        if wave_paths:
+            assert info["waves"] > 3
+        for job, img in zip(jobs, imgs):
+            want = _single(job, opts, info["walk"])
+            assert np.isfinite(img).all()
+            assert np.allclose(img, want, rtol=1e-5, atol=1e-6), job.scene.packed.prim_count
+        # a second run of the same graph adds the same passes again
+        br.run()
+        for img, again in zip(imgs, br.images()):
+            assert np.allclose(again, 2 * img, rtol=1e-5, atol=1e-6)
+    for j in jobs:
+        j.scene.close()
+
+
+def test_batch_progressive_frames(scenes):
+    """Replaying with new first frames renders the next passes (progressive refinement)."""
+    opts = ct.TraceOptions(max_bounces=6, russian_roulette=False, nee=True)
+    jobs = _jobs(scenes[:3], spp=2)
+    with ct.BatchRenderer(jobs, opts, wave_paths=900) as br:
+        br.run()
+        br.set_first_frames([j.seed * 7919 + 2 for j in jobs])
+        br.run()
+        got = br.images()
+        walk = br.info()["walk"]
+    from caustic import _native
+
+    for job, img in zip(jobs, got):
+        _native.check(job.scene._lib.ct_scene_set_option(job.scene.handle, 1, walk))
+        four = ct.render_image(job.scene, job.frame, ct.RenderOptions(
+            max_bounces=6, russian_roulette=False, nee=True, width=job.width, height=job.height, spp=4,
+            seed=job.seed))
+        assert np.allclose(img / 2, four, rtol=1e-5, atol=1e-6)
+        job.scene.close()
+
+
+def test_batch_rejects_bad_jobs(scenes):
+    opts = ct.TraceOptions()
+    jobs = _jobs(scenes[:1])
+    with pytest.raises(ct.CausticError):
+        ct.BatchRenderer(jobs, opts, walk=1)
+    jobs[0].scene.close()
