@@ -6,6 +6,13 @@ Workloads
             (4,194,304 samples). Metric: Msamples/s.
   traversal 1,000,000-triangle soup, 16,777,216 rays; a step is one
             intersectClosest batch over all rays. Metric: Mrays/s.
+  caustic   glass icosphere (327,680 triangles) among 64 spheres,
+            1920 x 1080, 64 spp, 12 bounces, Russian roulette on.
+  batched   256 scenes rendered by one CUDA graph, against the same jobs as
+            consecutive plain renders.
+  served    a request trace through the continuous-batching server, against
+            one plain renderImage per request (throughput all queued at
+            once; p50/p99 latency under Poisson arrivals).
 
 `value` is device time with inputs resident in HBM (CUDA events on the
 launching stream, max over ranks); `e2e` is the same metric through the
@@ -50,8 +57,9 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["cornell", "traversal", "caustic", "batched"], default="cornell")
+    ap.add_argument("--workload", choices=["cornell", "traversal", "caustic", "batched", "served"], default="cornell")
     ap.add_argument("--jobs", type=int, default=256, help="batched: number of scenes")
+    ap.add_argument("--requests", type=int, default=128, help="served: number of requests")
     ap.add_argument("--small", action="store_true", help="reduced sizes for profiling captures")
     ap.add_argument("--rays", type=int, default=0, help="traversal: trace only this many rays (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -643,6 +651,122 @@ def run_batched(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def served_inputs(count: int, small: bool, rank: int):
+    """Scene pool and request trace of the served workload. Pool: the 256
+    batched-workload soups, the unit Cornell box and the caustic scene.
+    Requests: `count`, each drawing a scene from the pool, a square side in
+    128..1024 (multiples of 128) and a target spp log-uniform in [1, 256]
+    (Rng(4242 + rank)); arrivals Poisson of mean gap 1 (rescaled by the caller)."""
+    import concurrent.futures as cf
+
+    import caustic as ct
+    from caustic.serve import poisson_requests
+
+    soups = ct.batch_workload(32 if small else 256, max_tris=20_000 if small else 200_000)
+    pool = {"cornell": ct.cornell_unit_box(), "caustic": ct.caustic_scene(level=5 if small else 7)}
+    pool.update({f"soup{i}": s for i, (s, _, _) in enumerate(soups)})
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        packed = dict(zip(pool, ex.map(ct.pack_scene, pool.values())))
+    frames = {k: (lambda a, cam=s.camera: ct.camera_frame(cam, a)) for k, s in pool.items()}
+    sides = (128, 256, 384) if small else tuple(range(128, 1025, 128))
+    reqs = poisson_requests(list(pool), frames, count, rate=1.0, seed=4242 + rank, sides=sides,
+                            max_spp=64 if small else 256)
+    return packed, reqs
+
+
+def run_served(args, rank, world):
+    """Served form: a request trace through the continuous-batching server
+    against the same trace as one plain renderImage per request, first all
+    queued at once (throughput), then with Poisson arrivals (latency)."""
+    import copy
+
+    import torch
+
+    import caustic as ct
+    from caustic.serve import GpuExecutor, RenderServer, latency_stats, render_plain
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    device = torch.device("cuda", torch.cuda.current_device())
+    opts = ct.TraceOptions(max_bounces=8, russian_roulette=True, nee=True)
+    count = 32 if args.small else args.requests
+    packed, trace = served_inputs(count, args.small, rank)
+    dev = {k: ct.DeviceScene(p) for k, p in packed.items()}
+    samples = sum(r.pixels * r.spp for r in trace)
+
+    def at(reqs, rate):
+        # the trace's arrival pattern scaled to `rate` requests/s (rate=None: all at t=0)
+        out = copy.deepcopy(reqs)
+        for r in out:
+            r.arrival = 0.0 if rate is None else r.arrival / rate
+        return out
+
+    def served(rate=None):
+        ex = GpuExecutor(dev, opts)
+        srv = RenderServer(ex)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(ex.stream)
+        res = srv.serve(at(trace, rate), t0=t0)
+        e1.record(ex.stream)
+        torch.cuda.synchronize()
+        return res, time.perf_counter() - t0, e0.elapsed_time(e1) / 1e3, srv
+
+    def plain(rate=None):
+        t0 = time.perf_counter()
+        res = render_plain(dev, at(trace, rate), opts, t0=t0)
+        torch.cuda.synchronize()
+        return res, time.perf_counter() - t0
+
+    for _ in range(max(3, args.warmup)):
+        served()
+    plain()
+    torch.cuda.synchronize()
+    barrier(world)
+    walls, devs = [], []
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        for _ in range(args.steps):
+            res, wall, dev_t, srv = served()
+            walls.append(wall)
+            devs.append(dev_t)
+    t_dev = max_over_ranks(sum(devs), world, device)
+    t_wall = max_over_ranks(sum(walls), world, device)
+    _, t_plain = plain()
+    t_plain = max_over_ranks(t_plain, world, device)
+    value = samples * args.steps * world / t_dev / 1e6
+    plain_rate = samples * world / t_plain / 1e6
+    # latency under Poisson arrivals at 80% of the plain path's request capacity
+    rate = 0.8 * len(trace) / t_plain
+    res_s, _, _, srv_s = served(rate)
+    res_p, _ = plain(rate)
+    line = {
+        "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_dev * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, Rng of the reference)",
+        "config": {"workload": f"served: {len(trace)} requests over {len(dev)} resident scenes (batched-workload "
+                               f"soups, unit Cornell box, caustic scene), sides "
+                               f"{'128-384' if args.small else '128-1024'} squared, 1-{64 if args.small else 256} spp, "
+                               f"depth 8, continuous batching of progressive passes (8 Mi paths per step, two steps "
+                               f"in flight), all requests queued at t=0",
+                   "requests": len(trace), "scenes": len(dev), "samples_per_step": samples,
+                   "server_steps": srv.steps, "peak_device_bytes": srv.peak_bytes,
+                   "parallelism": f"replicas x{args.gpus}"},
+        "plain_sequential": {"value": plain_rate, "unit": "Msamples/s",
+                             "what": "the same requests as consecutive ct_render_image_device calls, one at a time"},
+        "speedup_vs_plain": value / plain_rate,
+        "latency": {"arrivals": f"Poisson, {rate:.1f} requests/s (80% of the plain path's capacity)",
+                    "served": latency_stats(res_s), "plain": latency_stats(res_p), "served_steps": srv_s.steps},
+        "clocks": clocks.summary(),
+        "e2e": {"value": samples * args.steps * world / t_wall / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(sum(r.buffer_bytes for r in trace)),
+                "what": "host clock around the whole serve loop: batch planning, launches, per-step synchronisation "
+                        "and the device-to-host read of every finished image; scenes stay resident"},
+    }
+    for d in dev.values():
+        d.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -659,6 +783,8 @@ def main():
             run_reference(args, rank, world)
         elif args.workload == "batched":
             run_batched(args, rank, world)
+        elif args.workload == "served":
+            run_served(args, rank, world)
         else:
             run_gpu(args, rank, world)
     finally:

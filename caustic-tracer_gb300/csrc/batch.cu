@@ -1,19 +1,24 @@
 // Batched rendering: many scenes, cameras and image sizes in one graph.
 //
 // A batch is a list of jobs (scene, camera, size, frame indices, passes, sum
-// buffer). Their paths are packed into waves of up to `wave_paths` paths: the
-// planner walks passes in order and appends each job's pass as one segment
-// (split across waves when it does not fit), opening a new wave whenever a
-// job would appear twice in one, so every wave holds at most one pass of any
-// pixel and per-pixel sums stay in pass order. All waves run on the shared
-// wavefront kernels (BATCH = true), each path finding its scene, sky, camera
-// and output through its job record. The full launch sequence of all waves is
-// captured once into a CUDA graph and replayed by every ct_batch_run; the
-// frame indices live in a device table, so progressive passes reuse the same
-// graph (ct_batch_set_first_frames).
+// buffer). Their paths are packed into waves of up to `wave_paths` paths. The
+// planner takes the jobs grouped by trace walk and then by scene (a wave runs
+// one walk's kernel; the paths in flight at any time touch few BVHs) and
+// appends each job's passes as chunks: as many whole passes as fit in the
+// open wave, laid out pass-major; a pass larger than a wave is split by pixel
+// ranges over several waves. A wave holds at most one chunk of any job, so
+// every pixel's samples are added in pass order by a single thread (the sum a
+// single-scene render computes). All waves run on the shared wavefront
+// kernels (BATCH = true), each path finding its scene, sky, camera and output
+// through its job record. ct_batch_run captures the full launch sequence of
+// all waves once into a CUDA graph and replays it; the frame indices live in
+// a device table, so progressive passes reuse the same graph
+// (ct_batch_set_first_frames). ct_batch_run_direct launches the same
+// sequence without a graph, for batches run once.
 #include <algorithm>
 #include <cstring>
 #include <new>
+#include <unordered_map>
 #include <vector>
 
 #include "profile.hpp"
@@ -29,51 +34,90 @@ struct ct_batch {
   std::vector<ct::SegDev> segs;            // all waves, host copy
   std::vector<uint32_t> seg_pass;          // pass number of each segment
   struct Wave {
-    uint32_t seg0, nsegs, paths;
+    uint32_t seg0, nsegs, paths, acc;
+    int walk;
   };
   std::vector<Wave> waves;
   uint64_t max_paths = 0, total_paths = 0;
-  ct::DeviceBuffer d_jobs, d_segs, d_paths;
+  void* d_paths = nullptr;  // job and chunk tables, then the path state (pool memory)
+  ct::JobDev* d_jobs = nullptr;
+  ct::SegDev* d_segs = nullptr;
   ct::WaveArgs base{};
   size_t counter_words = 0;
   bool segs_dirty = true;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   size_t graph_nodes = 0;
+  cudaEvent_t done = nullptr;  // recorded after every run
 };
 
 namespace ct {
 namespace {
 
 constexpr uint64_t kDefaultWavePaths = 8ull << 20;
-constexpr uint32_t kBatchSkipMaxNodes = 31;
+
+// Trace walk of job j's waves: the batch's walk, or (kWalkPerJob) the one its
+// scene uses alone.
+int job_walk(const ct_batch* b, uint32_t j) {
+  return b->walk != kWalkPerJob ? b->walk : integrator_walk_form(b->jobs[j].scene);
+}
 
 void plan(ct_batch* b, uint64_t cap) {
-  uint32_t max_passes = 0;
-  for (const ct_batch_job& j : b->jobs) max_passes = std::max<uint32_t>(max_passes, (uint32_t)j.passes);
-  std::vector<int64_t> last_wave(b->jobs.size(), -1);
-  auto open = [&]() { b->waves.push_back({(uint32_t)b->segs.size(), 0, 0}); };
+  const uint32_t n = (uint32_t)b->jobs.size();
+  // Jobs grouped by walk, then by scene (groups in order of first appearance).
+  std::vector<uint32_t> order(n), group(n);
+  std::vector<int> walk(n);
+  std::unordered_map<const ct_scene*, uint32_t> first_job;
+  for (uint32_t j = 0; j < n; j++) {
+    group[j] = first_job.emplace(b->jobs[j].scene, j).first->second;
+    walk[j] = job_walk(b, j);
+    order[j] = j;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+    return walk[x] != walk[y] ? walk[x] < walk[y] : group[x] < group[y];
+  });
+  int cur_walk = n ? walk[order[0]] : kWalkThread;
+  auto open = [&]() { b->waves.push_back({(uint32_t)b->segs.size(), 0, 0, 0, cur_walk}); };
+  auto add = [&](uint32_t j, uint32_t q, uint32_t passes, uint32_t pixel0, uint32_t npix) {
+    ct_batch::Wave& w = b->waves.back();
+    b->segs.push_back(SegDev{j, b->jobs[j].first_frame_index + q, pixel0, w.paths, npix, passes, w.acc, 0});
+    b->seg_pass.push_back(q);
+    w.nsegs++;
+    w.paths += passes * npix;
+    w.acc += npix;
+  };
   open();
-  for (uint32_t q = 0; q < max_passes; q++) {
-    for (uint32_t j = 0; j < b->jobs.size(); j++) {
-      const ct_batch_job& job = b->jobs[j];
-      if ((uint32_t)job.passes <= q) continue;
-      const uint32_t pixels = (uint32_t)job.width * (uint32_t)job.height;
-      uint32_t done = 0;
-      while (done < pixels) {
-        ct_batch::Wave* w = &b->waves.back();
-        if (last_wave[j] == (int64_t)b->waves.size() - 1 || w->paths >= cap) {
-          open();
-          w = &b->waves.back();
-        }
-        const uint32_t take = (uint32_t)std::min<uint64_t>(pixels - done, cap - w->paths);
-        b->segs.push_back(SegDev{j, job.first_frame_index + q, done, w->paths});
-        b->seg_pass.push_back(q);
-        w->nsegs++;
-        w->paths += take;
-        done += take;
-        last_wave[j] = (int64_t)b->waves.size() - 1;
+  for (uint32_t j : order) {
+    const ct_batch_job& job = b->jobs[j];
+    if (walk[j] != cur_walk) {  // waves never mix walks
+      cur_walk = walk[j];
+      if (b->waves.back().nsegs) open();
+      b->waves.back().walk = cur_walk;
+    }
+    const uint64_t pixels = (uint64_t)job.width * (uint64_t)job.height;
+    const uint32_t P = (uint32_t)job.passes;
+    uint32_t q = 0, done = 0;  // next pass; pixels of pass q already placed
+    bool here = false;         // the open wave already holds a chunk of job j
+    while (q < P) {
+      if (here || b->waves.back().paths >= cap) {
+        open();
+        here = false;
       }
+      const uint64_t room = cap - b->waves.back().paths;
+      if (done == 0 && pixels <= room) {  // whole passes
+        const uint32_t np = (uint32_t)std::min<uint64_t>(P - q, room / pixels);
+        add(j, q, np, 0, (uint32_t)pixels);
+        q += np;
+      } else if (done == 0 && pixels <= cap) {  // a whole pass fits in a fresh wave
+        open();
+        continue;
+      } else {  // a pass larger than a wave, split by pixel ranges
+        const uint32_t take = (uint32_t)std::min<uint64_t>(pixels - done, room);
+        add(j, q, 1, done, take);
+        done += take;
+        if (done == pixels) done = 0, q++;
+      }
+      here = true;
     }
   }
   if (b->waves.back().nsegs == 0) b->waves.pop_back();
@@ -89,18 +133,19 @@ ct_status enqueue_all(ct_batch* b, cudaStream_t s) {
   const int32_t B = b->opts.max_bounces;
   for (const auto& wv : b->waves) {
     WaveArgs a = b->base;
-    a.segs = b->d_segs.as<SegDev>() + wv.seg0;
+    a.segs = b->d_segs + wv.seg0;
     a.nsegs = wv.nsegs;
     a.paths = wv.paths;
+    a.acc_items = wv.acc;
     CT_CUDA(cudaMemsetAsync(a.counts, 0, b->counter_words * 4, s));
     k_generate<true><<<g.gen, kBlock, 0, s>>>(a);
     WaveArgs w = a;
     for (int32_t bounce = 0; bounce <= B; bounce++) {
-      launch_trace<true>(b->walk, w, bounce, s);
+      launch_trace<true>(wv.walk, w, bounce, s);
       k_shade<true><<<g.shade, kBlock, 0, s>>>(w, bounce);
       std::swap(w.cur, w.next);
     }
-    launch_trace<true>(b->walk, w, B + 1, s);
+    launch_trace<true>(wv.walk, w, B + 1, s);
     k_accumulate_batch<<<g.acc, kBlock, 0, s>>>(a);
   }
   CT_CUDA(cudaGetLastError());
@@ -113,11 +158,11 @@ void destroy(ct_batch* b) {
   cudaGetDevice(&prev);
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->done) cudaEventSynchronize(b->done);  // the last run, on whatever stream it used
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  b->d_jobs.release(nullptr);
-  b->d_segs.release(nullptr);
-  b->d_paths.release(nullptr);
+  if (b->d_paths) path_free(b->d_paths, b->stream);  // the runs are done: back to the pool at once
+  if (b->done) cudaEventDestroy(b->done);
   if (b->stream) cudaStreamDestroy(b->stream);
   cudaSetDevice(prev);
   delete b;
@@ -126,27 +171,25 @@ void destroy(ct_batch* b) {
 ct_status create(const ct_batch_job* jobs, uint32_t count, const ct_trace_options* o, int64_t wave_paths,
                  int32_t walk, ct_batch** out) {
   CT_CHECK_ARG(jobs != nullptr && count > 0 && o != nullptr && out != nullptr, "NULL argument or empty batch");
-  CT_CHECK_ARG(walk == -1 || walk == 0 || walk == 2, "batch walk %d must be -1 (auto), 0 or 2", walk);
+  CT_CHECK_ARG(walk >= -1 && walk <= 2, "batch walk %d must be -1 (per job), 0, 1 or 2", walk);
   CT_CHECK_ARG(wave_paths >= 0 && wave_paths <= (1ll << 30), "wave_paths %lld outside [0, 2^30]", (long long)wave_paths);
   const int device = jobs[0].scene ? jobs[0].scene->device : -1;
-  bool all_small = true;
   for (uint32_t i = 0; i < count; i++) {
     const ct_batch_job& j = jobs[i];
     CT_CHECK_ARG(j.scene != nullptr && j.accum != nullptr, "job %u: NULL scene or accum", i);
     CT_CHECK_ARG(j.scene->device == device, "job %u: scene lives on device %d, job 0 on %d", i, j.scene->device, device);
     CT_CHECK_ARG(j.passes >= 0, "job %u: passes %d is negative", i, j.passes);
-    if (walk == 0) CT_CHECK_ARG(j.scene->depth <= ctk::kStackSize, "job %u: tree too deep for the ordered walk", i);
+    if (walk == 0 || walk == 1)
+      CT_CHECK_ARG(j.scene->depth <= ctk::kStackSize, "job %u: tree too deep for the ordered walk", i);
     ct_status st = check_options(&j.frame, j.width, j.height, o->max_bounces);
     if (st != CT_OK) return fail(st, "job %u: %s", i, last_error());
-    all_small = all_small && j.scene->node_count <= kBatchSkipMaxNodes;
-    if (j.scene->depth > ctk::kStackSize) all_small = true;  // deep trees need the stackless walk
   }
   const uint64_t cap = wave_paths > 0 ? (uint64_t)wave_paths : kDefaultWavePaths;
   ct_batch* b = new (std::nothrow) ct_batch();
   if (!b) return fail(CT_ERR_OUT_OF_MEMORY, "ct_batch_create: host allocation failed");
   b->device = device;
   b->opts = *o;
-  b->walk = walk >= 0 ? walk : (all_small ? kWalkSkip : kWalkThread);
+  b->walk = walk >= 0 ? walk : kWalkPerJob;
   b->jobs.assign(jobs, jobs + count);
   auto bail = [&](ct_status code) {
     destroy(b);
@@ -164,6 +207,11 @@ ct_status create(const ct_batch_job* jobs, uint32_t count, const ct_trace_option
       b->stream = nullptr;
       return bail(fail(CT_ERR_CUDA, "ct_batch_create: %s", cudaGetErrorString(err)));
     }
+    err = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (err != cudaSuccess) {
+      b->done = nullptr;
+      return bail(fail(CT_ERR_CUDA, "ct_batch_create: %s", cudaGetErrorString(err)));
+    }
   }
   std::vector<JobDev> host_jobs(count);
   for (uint32_t i = 0; i < count; i++) {
@@ -178,24 +226,26 @@ ct_status create(const ct_batch_job* jobs, uint32_t count, const ct_trace_option
   const uint64_t cap_paths = std::max<uint64_t>(1, b->max_paths);
   const size_t q = cap_paths * sizeof(float4), w4 = cap_paths * 4;
   b->counter_words = wave_counter_words(o->max_bounces);
-  const size_t bytes = 10 * q + 6 * w4 + b->counter_words * 4 + 20 * 256;
+  const size_t jobs_bytes = host_jobs.size() * sizeof(JobDev), segs_bytes = b->segs.size() * sizeof(SegDev);
+  const size_t bytes = jobs_bytes + segs_bytes + 10 * q + 4 * w4 + b->counter_words * 4 + 21 * 256;
   ct_status st;
-  if ((st = b->d_jobs.reserve(host_jobs.size() * sizeof(JobDev), nullptr)) != CT_OK ||
-      (st = b->d_segs.reserve(std::max<size_t>(1, b->segs.size()) * sizeof(SegDev), nullptr)) != CT_OK ||
-      (st = b->d_paths.reserve(bytes, nullptr)) != CT_OK)
-    return bail(st);
-  {
-    cudaError_t err = cudaMemcpyAsync(b->d_jobs.ptr, host_jobs.data(), host_jobs.size() * sizeof(JobDev),
-                                      cudaMemcpyHostToDevice, b->stream);
-    if (err == cudaSuccess) err = cudaStreamSynchronize(b->stream);
-    if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "batch upload: %s", cudaGetErrorString(err)));
-  }
-  char* base = b->d_paths.as<char>();
+  if ((st = path_alloc(device, bytes, b->stream, &b->d_paths)) != CT_OK) return bail(st);
+  char* base = static_cast<char*>(b->d_paths);
   auto take = [&](size_t n) {
     char* p = base;
     base += (n + 255) & ~size_t(255);
     return p;
   };
+  b->d_jobs = (JobDev*)take(jobs_bytes);
+  b->d_segs = (SegDev*)take(segs_bytes);
+  {  // both tables before the first run (a later ct_batch_set_first_frames re-uploads the chunks in stream order)
+    cudaError_t err = cudaMemcpyAsync(b->d_jobs, host_jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, b->stream);
+    if (err == cudaSuccess && segs_bytes)
+      err = cudaMemcpyAsync(b->d_segs, b->segs.data(), segs_bytes, cudaMemcpyHostToDevice, b->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(b->stream);
+    if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "batch upload: %s", cudaGetErrorString(err)));
+    b->segs_dirty = false;
+  }
   WaveArgs& a = b->base;
   a.cur = Queue{(float4*)take(q), (float4*)take(q), (float4*)take(q), (uint32_t*)take(w4)};
   a.next = Queue{(float4*)take(q), (float4*)take(q), (float4*)take(q), (uint32_t*)take(w4)};
@@ -203,10 +253,8 @@ ct_status create(const ct_batch_job* jobs, uint32_t count, const ct_trace_option
   a.radiance = (float4*)take(q);
   a.hit_prim = (int32_t*)take(w4);
   a.hit_t = (float*)take(w4);
-  a.path_job = (uint32_t*)take(w4);
-  a.path_pixel = (uint32_t*)take(w4);
   a.counts = (uint32_t*)take(b->counter_words * 4);
-  a.jobs = b->d_jobs.as<JobDev>();
+  a.jobs = b->d_jobs;
   a.max_bounces = o->max_bounces;
   a.rr = o->russian_roulette;
   a.nee = o->nee;
@@ -214,13 +262,20 @@ ct_status create(const ct_batch_job* jobs, uint32_t count, const ct_trace_option
   return CT_OK;
 }
 
-ct_status run(ct_batch* b, cudaStream_t s) {
+ct_status run(ct_batch* b, cudaStream_t s, bool direct) {
   CT_CUDA(cudaSetDevice(b->device));
   if (b->segs_dirty && !b->segs.empty()) {
-    CT_CUDA(cudaMemcpyAsync(b->d_segs.ptr, b->segs.data(), b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, s));
+    CT_CUDA(cudaMemcpyAsync(b->d_segs, b->segs.data(), b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, s));
     b->segs_dirty = false;
   }
   if (b->waves.empty()) return CT_OK;
+  if (direct) {  // launches straight onto s (no capture): for one-shot batches
+    ProfScope ps("batch_direct", s);
+    ct_status st = enqueue_all(b, s);
+    if (st != CT_OK) return st;
+    CT_CUDA(cudaEventRecord(b->done, s));
+    return CT_OK;
+  }
   if (!b->exec) {
     (void)grids<true>();  // occupancy queries before capture
     cudaStream_t cap = b->stream;
@@ -238,8 +293,11 @@ ct_status run(ct_batch* b, cudaStream_t s) {
     CT_CUDA(cudaGraphGetNodes(graph, nullptr, &b->graph_nodes));
     CT_CUDA(cudaGraphInstantiate(&b->exec, graph, 0));
   }
-  ProfScope ps("batch_graph", s);
-  CT_CUDA(cudaGraphLaunch(b->exec, s));
+  {
+    ProfScope ps("batch_graph", s);
+    CT_CUDA(cudaGraphLaunch(b->exec, s));
+  }
+  CT_CUDA(cudaEventRecord(b->done, s));
   return CT_OK;
 }
 
@@ -271,7 +329,13 @@ ct_status ct_batch_set_first_frames(ct_batch* batch, const uint32_t* first_frame
 ct_status ct_batch_run(ct_batch* batch, void* stream) {
   ct::clear_error();
   CT_CHECK_ARG(batch != nullptr, "batch is NULL");
-  return ct::run(batch, stream ? static_cast<cudaStream_t>(stream) : batch->stream);
+  return ct::run(batch, stream ? static_cast<cudaStream_t>(stream) : batch->stream, false);
+}
+
+ct_status ct_batch_run_direct(ct_batch* batch, void* stream) {
+  ct::clear_error();
+  CT_CHECK_ARG(batch != nullptr, "batch is NULL");
+  return ct::run(batch, stream ? static_cast<cudaStream_t>(stream) : batch->stream, true);
 }
 
 ct_status ct_batch_info(const ct_batch* batch, uint32_t* waves, uint64_t* paths, uint64_t* graph_nodes,

@@ -2,7 +2,10 @@
 
 Each translation unit is compiled by its own nvcc process (in parallel), then
 linked into one shared library. Host C++ is compiled with -ffp-contract=off so
-the packer's float64 arithmetic rounds exactly like the reference's.
+the packer's float64 arithmetic rounds exactly like the reference's. Device
+code is compiled with -fmad=false: the compiler fuses no multiply-add on its
+own (its choice could differ between kernels that inline the same function),
+and hot code writes the fused forms it wants with __fmaf_rn.
 """
 from __future__ import annotations
 
@@ -35,7 +38,7 @@ def _compile(src: str, obj: pathlib.Path) -> None:
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
               f"-I{HERE}", f"-I{PKG.parent / 'include'}"]
     if src.endswith(".cu"):
-        cmd = [nvcc(), ARCH, "-lineinfo", "-Xptxas", "-v" if os.environ.get("CT_PTXAS_VERBOSE") else "-O3",
+        cmd = [nvcc(), ARCH, "-lineinfo", "-fmad=false", "-Xptxas", "-v" if os.environ.get("CT_PTXAS_VERBOSE") else "-O3",
                *common, "-c", str(path), "-o", str(obj)]
     else:
         cmd = [nvcc(), "-x", "c++", *common, "-c", str(path), "-o", str(obj)]

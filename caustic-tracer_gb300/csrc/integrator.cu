@@ -43,17 +43,15 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   const size_t q_bytes = cap * sizeof(float4);
   const size_t counter_words = wave_counter_words(B);
   const size_t bytes = 10 * q_bytes + cap * 8 + counter_words * 4 + 16 * 256;
-  if (s->paths.buf.bytes < bytes) {
-    DeviceBuffer cached;
-    if (path_cache_take(s->device, bytes, cached)) {
-      s->paths.buf.release(&s->device_bytes);
-      s->paths.buf = cached;
-      s->device_bytes += cached.bytes;
-    }
-  }
-  ct_status st = s->paths.buf.reserve(bytes, &s->device_bytes);
+  void* buf = nullptr;
+  ct_status st = path_alloc(s->device, bytes, stream, &buf);
   if (st != CT_OK) return st;
-  char* base = s->paths.buf.as<char>();
+  struct Release {  // back to the pool, in stream order, on every return
+    void* p;
+    cudaStream_t s;
+    ~Release() { path_free(p, s); }
+  } release{buf, stream};
+  char* base = static_cast<char*>(buf);
   auto take = [&](size_t n) {
     char* p = base;
     base += (n + 255) & ~size_t(255);

@@ -49,7 +49,12 @@ struct V3f {
   float x, y, z;
 };
 __device__ __forceinline__ V3f mk(float x, float y, float z) { return V3f{x, y, z}; }
-__device__ __forceinline__ float dot3(V3f a, V3f b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// Fused forms are written out (device code is compiled with -fmad=false).
+__device__ __forceinline__ float dot3(V3f a, V3f b) { return __fmaf_rn(a.x, b.x, __fmaf_rn(a.y, b.y, a.z * b.z)); }
+// a + b * s per component
+__device__ __forceinline__ V3f madd3(V3f a, V3f b, float s) {
+  return mk(__fmaf_rn(b.x, s, a.x), __fmaf_rn(b.y, s, a.y), __fmaf_rn(b.z, s, a.z));
+}
 __device__ __forceinline__ V3f normalize3(V3f a) {
   const float l2 = dot3(a, a);
   const float inv = l2 > 0.0f ? rsqrtf(l2) : 0.0f;
@@ -75,7 +80,7 @@ __device__ __forceinline__ V3f cosine_hemisphere(V3f n, float u1, float u2) {
   const float z = sqrtf(u1 < 1.0f ? 1.0f - u1 : 0.0f);
   V3f t, b;
   basis(n, t, b);
-  return normalize3(mk(t.x * x + b.x * y + n.x * z, t.y * x + b.y * y + n.y * z, t.z * x + b.z * y + n.z * z));
+  return normalize3(madd3(madd3(mk(n.x * z, n.y * z, n.z * z), b, y), t, x));
 }
 
 // unitVectorInto (materials.ts:67-74)
@@ -107,11 +112,11 @@ __device__ __forceinline__ float dielectric_reflectance(float cos_i, float eta_i
 // metalInto (materials.ts:102-124)
 __device__ __forceinline__ V3f metal_dir(V3f d, V3f n, float rough, float u1, float u2, float u3) {
   const float k = 2.0f * dot3(d, n);
-  V3f r = mk(d.x - k * n.x, d.y - k * n.y, d.z - k * n.z);
+  V3f r = madd3(d, n, -k);
   if (rough > 0.0f) {
     const V3f u = unit_vector(u1, u2);
     const float rad = cbrtf(u3) * rough;
-    r = mk(r.x + u.x * rad, r.y + u.y * rad, r.z + u.z * rad);
+    r = madd3(r, u, rad);
   }
   return normalize3(r);
 }
@@ -126,11 +131,11 @@ __device__ __forceinline__ V3f dielectric_dir(V3f d, V3f n, float ior, bool fron
   const float sin2t = eta * eta * (1.0f - cos_i * cos_i);
   if (u < refl || sin2t > 1.0f) {
     const float k = 2.0f * dot3(d, n);
-    return mk(d.x - k * n.x, d.y - k * n.y, d.z - k * n.z);
+    return madd3(d, n, -k);
   }
   const float cos_t = sqrtf(1.0f - sin2t);
   const float s = eta * cos_i - cos_t;
-  return normalize3(mk(d.x * eta + n.x * s, d.y * eta + n.y * s, d.z * eta + n.z * s));
+  return normalize3(madd3(mk(d.x * eta, d.y * eta, d.z * eta), n, s));
 }
 
 // powerHeuristic (materials.ts:169-174)

@@ -47,38 +47,49 @@ void DeviceBuffer::release(size_t* total_bytes) {
 }
 
 namespace {
-std::mutex g_cache_mu;
-constexpr int kCacheDevices = 64;
-DeviceBuffer g_path_cache[kCacheDevices];
+std::mutex g_pool_mu;
+constexpr int kPoolDevices = 64;
+cudaMemPool_t g_pool[kPoolDevices] = {};
 }  // namespace
 
-void path_cache_put(int device, DeviceBuffer& b) {
-  if (!b.ptr) return;
-  std::lock_guard<std::mutex> guard(g_cache_mu);
-  if (device < 0 || device >= kCacheDevices) {
-    b.release(nullptr);
-    return;
+ct_status path_pool(int device, cudaMemPool_t* out) {
+  CT_CHECK_ARG(device >= 0 && device < kPoolDevices, "device %d outside [0, %d)", device, kPoolDevices);
+  std::lock_guard<std::mutex> guard(g_pool_mu);
+  if (!g_pool[device]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t pool = nullptr;
+    CT_CUDA(cudaMemPoolCreate(&pool, &props));
+    uint64_t keep = ~0ull;  // freed blocks stay in the pool for the next render
+    cudaError_t err = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (err != cudaSuccess) {
+      cudaMemPoolDestroy(pool);
+      return fail(CT_ERR_CUDA, "cudaMemPoolSetAttribute: %s", cudaGetErrorString(err));
+    }
+    g_pool[device] = pool;
   }
-  DeviceBuffer& slot = g_path_cache[device];
-  if (slot.bytes >= b.bytes) {
-    b.release(nullptr);
-  } else {
-    slot.release(nullptr);
-    slot = b;
-    b.ptr = nullptr;
-    b.bytes = 0;
-  }
+  *out = g_pool[device];
+  return CT_OK;
 }
 
-bool path_cache_take(int device, size_t want, DeviceBuffer& out) {
-  std::lock_guard<std::mutex> guard(g_cache_mu);
-  if (device < 0 || device >= kCacheDevices) return false;
-  DeviceBuffer& slot = g_path_cache[device];
-  if (!slot.ptr || slot.bytes < want) return false;
-  out = slot;
-  slot.ptr = nullptr;
-  slot.bytes = 0;
-  return true;
+ct_status path_alloc(int device, size_t bytes, cudaStream_t s, void** out) {
+  *out = nullptr;
+  cudaMemPool_t pool = nullptr;
+  ct_status st = path_pool(device, &pool);
+  if (st != CT_OK) return st;
+  const cudaError_t err = cudaMallocFromPoolAsync(out, bytes, pool, s);
+  if (err != cudaSuccess) {
+    *out = nullptr;
+    (void)cudaGetLastError();
+    return fail(CT_ERR_OUT_OF_MEMORY, "path state of %zu bytes: %s", bytes, cudaGetErrorString(err));
+  }
+  return CT_OK;
+}
+
+void path_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
 }
 
 namespace {
@@ -200,7 +211,6 @@ void destroy(ct_scene* s) {
   cudaGetDevice(&prev);
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
-  path_cache_put(s->device, s->paths.buf);
   for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->pairs, &s->mats, &s->lights, &s->prim_object, &s->io,
                           &s->counters})
     b->release(&s->device_bytes);

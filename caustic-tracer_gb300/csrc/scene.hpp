@@ -33,18 +33,17 @@ struct DeviceBuffer {
   }
 };
 
-// Per-scene wavefront state of the integrator (see integrator.cu).
-struct PathState {
-  DeviceBuffer buf;          // all per-path arrays, carved from one allocation
-  uint64_t capacity = 0;     // paths the buffer holds
-};
+// Path state (wavefront queues and per-path arrays) comes from one
+// stream-ordered memory pool per device: a render or batch allocates it on
+// its stream and frees it there when its work is queued, and the pool keeps
+// freed blocks for the next one, so renders neither hold memory between
+// calls nor pay for cudaMalloc/cudaFree (which would wait for the device).
+ct_status path_alloc(int device, size_t bytes, cudaStream_t s, void** out);
+void path_free(void* p, cudaStream_t s);
 
-// Path-state buffers outlive their scenes: ct_scene_destroy hands the buffer
-// to a per-device cache (the largest one is kept) and the next scene on that
-// device adopts it, so a create/render/destroy cycle does not allocate and
-// free hundreds of megabytes each time.
-void path_cache_put(int device, DeviceBuffer& b);
-bool path_cache_take(int device, size_t want, DeviceBuffer& out);
+// Trace walk the single-scene integrator uses for `s` (0 ordered per thread,
+// 1 ordered persistent, 2 stackless skip-link); see integrator.cu.
+int integrator_walk_form(const ct_scene* s);
 
 }  // namespace ct
 
@@ -63,7 +62,6 @@ struct ct_scene {
   // Staging for host-pointer entry points and per-call counters.
   ct::DeviceBuffer io;
   ct::DeviceBuffer counters;  // uint32 fp64-fallback counter and error flag
-  ct::PathState paths;
   size_t device_bytes = 0;
 
   // Tuning options (ct_scene_set_option): integrator walk form (-1 = chosen

@@ -287,25 +287,30 @@ constexpr float kReportRel = 1e-6f;
 
 // Plain float32 forms of the reference's tests (same decisions, float32
 // rounding), for the path integrator whose parity is statistical. The
-// candidate must also be nearer than `closest`.
+// candidate must also be nearer than `closest`. Every fused multiply-add is
+// written out (the library is compiled with -fmad=false), so each kernel
+// that inlines these tests rounds them identically.
+__device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+
 __device__ __forceinline__ bool tri_fast(const RayF& r, float4 a4, float4 b4, float4 c4, float closest, Cand& c) {
   const float e1x = b4.x - a4.x, e1y = b4.y - a4.y, e1z = b4.z - a4.z;
   const float e2x = c4.x - a4.x, e2y = c4.y - a4.y, e2z = c4.z - a4.z;
-  const float px = r.dy * e2z - r.dz * e2y;
-  const float py = r.dz * e2x - r.dx * e2z;
-  const float pz = r.dx * e2y - r.dy * e2x;
-  const float det = e1x * px + e1y * py + e1z * pz;
+  const float px = fm(r.dy, e2z, -mul(r.dz, e2y));
+  const float py = fm(r.dz, e2x, -mul(r.dx, e2z));
+  const float pz = fm(r.dx, e2y, -mul(r.dy, e2x));
+  const float det = fm(e1x, px, fm(e1y, py, mul(e1z, pz)));
   if (det > -1e-12f && det < 1e-12f) return false;
   const float inv = 1.0f / det;
   const float tx = r.ox - a4.x, ty = r.oy - a4.y, tz = r.oz - a4.z;
-  const float u = (tx * px + ty * py + tz * pz) * inv;
+  const float u = mul(fm(tx, px, fm(ty, py, mul(tz, pz))), inv);
   if (u < 0.0f || u > 1.0f) return false;
-  const float qx = ty * e1z - tz * e1y;
-  const float qy = tz * e1x - tx * e1z;
-  const float qz = tx * e1y - ty * e1x;
-  const float v = (r.dx * qx + r.dy * qy + r.dz * qz) * inv;
+  const float qx = fm(ty, e1z, -mul(tz, e1y));
+  const float qy = fm(tz, e1x, -mul(tx, e1z));
+  const float qz = fm(tx, e1y, -mul(ty, e1x));
+  const float v = mul(fm(r.dx, qx, fm(r.dy, qy, mul(r.dz, qz))), inv);
   if (v < 0.0f || u + v > 1.0f) return false;
-  const float t = (e2x * qx + e2y * qy + e2z * qz) * inv;
+  const float t = mul(fm(e2x, qx, fm(e2y, qy, mul(e2z, qz))), inv);
   if (t <= r.tmin || t >= closest) return false;
   c.t = t;
   c.e = 0.0f;
@@ -316,9 +321,10 @@ __device__ __forceinline__ bool tri_fast(const RayF& r, float4 a4, float4 b4, fl
 
 __device__ __forceinline__ bool sphere_fast(const RayF& r, float4 c4, float rad, float closest, Cand& c) {
   const float lx = r.ox - c4.x, ly = r.oy - c4.y, lz = r.oz - c4.z;
-  const float a = r.dx * r.dx + r.dy * r.dy + r.dz * r.dz;
-  const float hb = lx * r.dx + ly * r.dy + lz * r.dz;
-  const float disc = hb * hb - a * (lx * lx + ly * ly + lz * lz - rad * rad);
+  const float a = fm(r.dx, r.dx, fm(r.dy, r.dy, mul(r.dz, r.dz)));
+  const float hb = fm(lx, r.dx, fm(ly, r.dy, mul(lz, r.dz)));
+  const float cc = fm(lx, lx, fm(ly, ly, fm(lz, lz, -mul(rad, rad))));
+  const float disc = fm(hb, hb, -mul(a, cc));
   if (disc < 0.0f) return false;
   const float s = sqrtf(disc);
   float t = (-hb - s) / a;
@@ -516,8 +522,10 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
 // answered is refilled as soon as a quarter of the warp is idle, so lanes
 // keep stepping instead of waiting for the warp's slowest ray. All 32 lanes
 // of every warp must call this (the block size is a multiple of 32).
-template <bool EXACT, class Begin, class Finish>
-__device__ __forceinline__ void walk_persistent(const SceneDev& s, uint32_t* counter, uint32_t total, Begin begin,
+// `s` is the scene the lane walks: a fixed scene, or (queries of many scenes)
+// a per-lane copy that begin() replaces with the new query's scene.
+template <bool EXACT, class Scene, class Begin, class Finish>
+__device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uint32_t total, Begin begin,
                                                 Finish finish, uint32_t& fallbacks) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt_mask = (1u << lane) - 1u;

@@ -49,7 +49,8 @@ struct Queue {
   uint32_t* job;  // BATCH: job of each slot
 };
 
-// One NEE shadow ray: a = origin.xyz, tmax; b = dir.xyz, path id; c = contribution.rgb.
+// One NEE shadow ray: a = origin.xyz, tmax; b = dir.xyz, path id;
+// c = contribution.rgb, job (BATCH).
 struct ShadowQueue {
   float4* a;
   float4* b;
@@ -70,10 +71,13 @@ struct JobDev {
   float* accum;
 };
 
-// Paths [path0, next segment's path0) of a wave: pixels pixel0.. of `job` in
-// the pass with frame index `frame_index`.
+// One chunk of a wave: `passes` consecutive passes (frame indices
+// frame_index, frame_index+1, ...) over pixels [pixel0, pixel0+npix) of `job`,
+// laid out pass-major at paths [path0, path0 + passes*npix). Its pixels are
+// accumulation items [acc0, acc0 + npix) of the wave. A wave holds at most
+// one chunk of any job, so no two chunks add to the same pixel.
 struct SegDev {
-  uint32_t job, frame_index, pixel0, path0;
+  uint32_t job, frame_index, pixel0, path0, npix, passes, acc0, pad;
 };
 
 struct WaveArgs {
@@ -92,8 +96,7 @@ struct WaveArgs {
   const JobDev* jobs;
   const SegDev* segs;
   uint32_t nsegs;
-  uint32_t* path_job;    // per path id
-  uint32_t* path_pixel;  // per path id
+  uint32_t acc_items;    // pixels of all chunks of the wave
 };
 
 // Counter words of a wave: [0, B+2) path queue sizes, [B+2, 2B+4) shadow
@@ -124,12 +127,14 @@ __device__ __forceinline__ uint32_t block_append(bool pred, uint32_t* counter, u
   return slot;
 }
 
-// Segment holding path p (segments are sorted by path0, the first at 0).
+// Chunk holding path p (KEY = path0) or accumulation item p (KEY = acc0);
+// chunks are sorted by both, the first at 0.
+template <uint32_t SegDev::*KEY>
 __device__ __forceinline__ uint32_t find_segment(const SegDev* segs, uint32_t nsegs, uint32_t p) {
   uint32_t lo = 0, hi = nsegs;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
-    if (__ldg(&segs[mid].path0) <= p) lo = mid;
+    if (__ldg(&(segs[mid].*KEY)) <= p) lo = mid;
     else hi = mid;
   }
   return lo;
@@ -142,17 +147,16 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
     uint32_t pixel, frame_index, width, height, job = 0;
     const ctk::FrameF* frame;
     if constexpr (BATCH) {
-      const SegDev& sg = a.segs[find_segment(a.segs, a.nsegs, p)];
+      const SegDev& sg = a.segs[find_segment<&SegDev::path0>(a.segs, a.nsegs, p)];
       job = sg.job;
-      pixel = sg.pixel0 + (p - sg.path0);
-      frame_index = sg.frame_index;
+      const uint32_t off = p - sg.path0, k = off / sg.npix;
+      pixel = sg.pixel0 + (off - k * sg.npix);
+      frame_index = sg.frame_index + k;
       const JobDev& j = a.jobs[job];
       width = j.width;
       height = j.height;
       frame = &j.frame;
       a.cur.job[p] = job;
-      a.path_job[p] = job;
-      a.path_pixel[p] = pixel;
     } else {
       const uint32_t pass = p / a.pixels;
       pixel = p - pass * a.pixels;
@@ -188,10 +192,13 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
 // Walk forms of the trace kernel (chosen per scene by the host):
 //   kWalkThread     ordered walk, one per thread in a grid-stride loop;
 //   kWalkPersistent ordered walk, lanes refill from a work counter as their
-//                   walks finish (pays off for deep trees; single scene only);
+//                   walks finish (pays off for deep trees);
 //   kWalkSkip       the reference's stackless skip-link walk (no stack; all
-//                   lanes visit nodes in the same order; for small trees).
-enum WalkForm : int { kWalkThread = 0, kWalkPersistent = 1, kWalkSkip = 2 };
+//                   lanes visit nodes in the same order; for small trees);
+//   kWalkPerJob     BATCH only, a planning mode: every wave holds jobs of one
+//                   walk, the one each job's scene uses alone, and runs that
+//                   walk's kernel.
+enum WalkForm : int { kWalkThread = 0, kWalkPersistent = 1, kWalkSkip = 2, kWalkPerJob = 3 };
 
 // Closest hits of the bounce-b path queue plus the shadow rays of bounce b-1.
 template <int FORM, bool BATCH>
@@ -211,13 +218,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_trace(WaveArgs a, int32_t bounce)
     }
     ctk::finish_ray(r);
   };
-  auto scene_of = [&](uint32_t i) -> const ctk::SceneDev& {
-    if constexpr (BATCH) {
-      const uint32_t job = i < n_ext ? a.cur.job[i] : a.path_job[__float_as_uint(a.shadow.b[i - n_ext].w)];
-      return a.jobs[job].scene;
-    } else {
-      return a.scene;
-    }
+  auto job_of = [&](uint32_t i) -> const JobDev& {
+    return a.jobs[i < n_ext ? a.cur.job[i] : __float_as_uint(a.shadow.c[i - n_ext].w)];
   };
   auto finish = [&](uint32_t i, ctk::Walk& w) {
     if (i < n_ext) {
@@ -234,6 +236,9 @@ __global__ void __launch_bounds__(kBlock, 8) k_trace(WaveArgs a, int32_t bounce)
       *L = l;
     }
   };
+  // A batch query copies its job's scene record into registers once, so the
+  // walk reads the base pointers as often as the single-scene kernel reads
+  // its kernel parameters.
   if constexpr (FORM == kWalkPersistent && !BATCH) {
     ctk::walk_persistent<false>(
         a.scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh,
@@ -242,12 +247,22 @@ __global__ void __launch_bounds__(kBlock, 8) k_trace(WaveArgs a, int32_t bounce)
           ctk::walk_begin(a.scene, w, i >= n_ext);
         },
         finish, fallbacks);
+  } else if constexpr (FORM == kWalkPersistent) {
+    ctk::SceneDev lane_scene = a.jobs[0].scene;
+    ctk::walk_persistent<false>(
+        lane_scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh,
+        [&](uint32_t i, ctk::Walk& w) {
+          load(i, w.r);
+          lane_scene = job_of(i).scene;
+          ctk::walk_begin(lane_scene, w, i >= n_ext);
+        },
+        finish, fallbacks);
   } else {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_ext + n_sh; i += stride) {
       ctk::Walk w;
       load(i, w.r);
-      const ctk::SceneDev& sc = scene_of(i);
+      const ctk::SceneDev sc = BATCH ? job_of(i).scene : a.scene;
       if constexpr (FORM == kWalkSkip) {
         w.h = ctk::HitF{-1, w.r.tmax, 0.0f, 0.0f, 0.0f};
         ctk::walk_stackless<false>(sc, w.r, w.h, i >= n_ext, fallbacks);
@@ -273,14 +288,12 @@ __global__ void __launch_bounds__(kBlock) k_shade(WaveArgs a, int32_t bounce) {
     uint32_t job = 0;
     float4 na = make_float4(0, 0, 0, 0), nb = na, nc = na, sa = na, sb = na, scol = na;
     if (i < n) {
-      const ctk::SceneDev* scp = &a.scene;
       const SkyF* sky = &a.sky;
       if constexpr (BATCH) {
         job = a.cur.job[i];
-        scp = &a.jobs[job].scene;
         sky = &a.jobs[job].sky;
       }
-      const ctk::SceneDev& sc = *scp;
+      const ctk::SceneDev sc = BATCH ? a.jobs[job].scene : a.scene;  // registers, loaded up front
       const bool use_nee = a.nee != 0 && sc.light_count > 0;
       const float4 qa = a.cur.a[i], qb = a.cur.b[i], qc = a.cur.c[i];
       uint32_t rng = __float_as_uint(qa.w);
@@ -301,7 +314,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(WaveArgs a, int32_t bounce) {
         const float t = a.hit_t[i];
         const float4* q = sc.prims + (size_t)prim * 4;
         const float4 q0 = __ldg(q);
-        const ctk::V3f p = ctk::mk(o.x + d.x * t, o.y + d.y * t, o.z + d.z * t);
+        const ctk::V3f p = ctk::madd3(o, d, t);
         ctk::V3f nrm;
         if (q0.w == 0.0f) {
           const float inv_r = 1.0f / __ldg(q + 1).x;
@@ -340,7 +353,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(WaveArgs a, int32_t bounce) {
               sa = make_float4(p.x, p.y, p.z, ls.dist * ctk::kShadowShorten);
               sb = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, __uint_as_float(pid));
               scol = make_float4(tr * ar * ls.emission.x * k, tg * ag * ls.emission.y * k,
-                                 tb * ab * ls.emission.z * k, 0.0f);
+                                 tb * ab * ls.emission.z * k, __uint_as_float(job));
             }
           }
           const float u1 = ctk::next_f(rng);
@@ -426,17 +439,23 @@ __global__ void __launch_bounds__(kBlock) k_accumulate(const float4* __restrict_
   }
 }
 
-// Batch: each path adds its sample to its job's pixel. A wave holds at most
-// one pass of any (job, pixel), so no two threads touch the same sum.
+// Batch: each pixel of each chunk adds its chunk's samples, in pass order,
+// to its job's sum (the same sequence of float additions as k_accumulate).
 __global__ void __launch_bounds__(kBlock) k_accumulate_batch(WaveArgs a) {
   const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.paths; p += stride) {
-    const float4 l = a.radiance[p];
-    if (!(isfinite(l.x) && isfinite(l.y) && isfinite(l.z))) continue;
-    float* acc = a.jobs[a.path_job[p]].accum + 3 * (size_t)a.path_pixel[p];
-    acc[0] += l.x;
-    acc[1] += l.y;
-    acc[2] += l.z;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.acc_items; i += stride) {
+    const SegDev& sg = a.segs[find_segment<&SegDev::acc0>(a.segs, a.nsegs, i)];
+    const uint32_t local = i - sg.acc0;
+    float* acc = a.jobs[sg.job].accum + 3 * (size_t)(sg.pixel0 + local);
+    float r = acc[0], g = acc[1], b = acc[2];
+    const float4* l = a.radiance + sg.path0 + local;
+    for (uint32_t k = 0; k < sg.passes; k++, l += sg.npix) {
+      const float4 v = *l;
+      if (isfinite(v.x) && isfinite(v.y) && isfinite(v.z)) r += v.x, g += v.y, b += v.z;
+    }
+    acc[0] = r;
+    acc[1] = g;
+    acc[2] = b;
   }
 }
 
@@ -456,7 +475,7 @@ int persistent_grid(K kernel) {
 
 template <bool BATCH>
 struct Grids {
-  int gen = 0, trace[3] = {0, 0, 0}, shade = 0, acc = 0;
+  int gen = 0, trace[4] = {0, 0, 0, 0}, shade = 0, acc = 0;
 };
 
 template <bool BATCH>
@@ -481,11 +500,11 @@ void launch_trace(int form, const WaveArgs& w, int32_t bounce, cudaStream_t stre
     case kWalkPersistent:
       k_trace<kWalkPersistent, BATCH><<<g.trace[kWalkPersistent], kBlock, 0, stream>>>(w, bounce);
       break;
-    case kWalkSkip:
-      k_trace<kWalkSkip, BATCH><<<g.trace[kWalkSkip], kBlock, 0, stream>>>(w, bounce);
-      break;
     default:
       k_trace<kWalkThread, BATCH><<<g.trace[kWalkThread], kBlock, 0, stream>>>(w, bounce);
+      break;
+    case kWalkSkip:
+      k_trace<kWalkSkip, BATCH><<<g.trace[kWalkSkip], kBlock, 0, stream>>>(w, bounce);
       break;
   }
 }

@@ -193,7 +193,10 @@ uint32_t ct_rng_stream(uint32_t seed_or_state, int32_t is_state, uint64_t n, int
  * tracer (tracer.ts:348, intersect.ts:202).                                 */
 ct_status ct_scene_create(const ct_packed_scene_view* ps, ct_scene** out);
 void ct_scene_destroy(ct_scene* scene);
-/* Device bytes held by the scene (for admission budgets). */
+/* Device bytes held by the scene (for admission budgets). Path state of a
+ * render or batch is not part of it: it comes from a per-device
+ * stream-ordered pool for the duration of the call's work, and the pool
+ * keeps its high-water mark for reuse (8 Mi paths in flight ~ 1.5 GiB).     */
 uint64_t ct_scene_device_bytes(const ct_scene* scene);
 
 /* Per-scene tuning knobs, set by callers or an autotuner. No counterpart in
@@ -256,7 +259,10 @@ ct_status ct_render_image_device(ct_scene* scene, const ct_camera_frame* frame,
  * the job's device sum buffer `accum` (width*height*3 floats). Results equal
  * those of the single-scene entry points for the same frame indices.
  * The paths of all jobs share waves of up to wave_paths paths (0 = 8 Mi);
- * walk selects the trace walk (-1 auto, 0 ordered, 2 stackless skip-link).
+ * walk selects the trace walk: -1 = each job the walk its scene uses alone
+ * (so every result equals its single-scene render bit for bit; a wave holds
+ * jobs of one walk), or 0 ordered per thread, 1 ordered with persistent lane
+ * refill, 2 stackless skip-link for all jobs. ct_batch_info reports 3 for -1.
  * The first ct_batch_run captures the whole launch sequence in a CUDA graph;
  * later runs replay it. Scenes must outlive the batch and must not be used
  * by other calls while a run is in flight.                                  */
@@ -278,6 +284,9 @@ ct_status ct_batch_create(const ct_batch_job* jobs, uint32_t count, const ct_tra
 ct_status ct_batch_set_first_frames(ct_batch* batch, const uint32_t* first_frame_index);
 /* Enqueues the batch on `stream` (NULL = the batch's own stream). */
 ct_status ct_batch_run(ct_batch* batch, void* stream);
+/* Same work launched directly, without capturing a graph: for batches run
+ * once (a serving step whose set of jobs changes every time).              */
+ct_status ct_batch_run_direct(ct_batch* batch, void* stream);
 ct_status ct_batch_info(const ct_batch* batch, uint32_t* waves, uint64_t* paths, uint64_t* graph_nodes,
                         int32_t* walk);
 void ct_batch_destroy(ct_batch* batch);

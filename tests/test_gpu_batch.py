@@ -17,13 +17,21 @@ def _jobs(scenes, spp=3):
     return jobs
 
 
-def _single(job, opts, walk):
+PER_JOB = 3  # ct_batch_info walk: every job walks as its scene does alone
+
+
+def _force_walk(scene, walk):
     # Same trace walk as the batch: in float32, walks that visit nodes in a
     # different order can break exact ties (a quad's shared diagonal) the
-    # other way, which changes a path but not the estimator.
+    # other way, which changes a path but not the estimator. A per-job batch
+    # needs no override (-1 keeps the scene's own choice).
     from caustic import _native
 
-    _native.check(job.scene._lib.ct_scene_set_option(job.scene.handle, 1, walk))
+    _native.check(scene._lib.ct_scene_set_option(scene.handle, 1, -1 if walk == PER_JOB else walk))
+
+
+def _single(job, opts, walk):
+    _force_walk(job.scene, walk)
     return ct.render_image(job.scene, job.frame, ct.RenderOptions(
         max_bounces=opts.max_bounces, russian_roulette=opts.russian_roulette, nee=opts.nee,
         width=job.width, height=job.height, spp=job.spp, seed=job.seed))
@@ -37,7 +45,7 @@ def scenes(native_lib):
     return out
 
 
-@pytest.mark.parametrize("wave_paths,walk", [(0, -1), (1000, -1), (777, 0), (5000, 2)])
+@pytest.mark.parametrize("wave_paths,walk", [(0, -1), (1000, -1), (777, 0), (5000, 2), (3000, 1)])
 def test_batch_equals_single_renders(scenes, wave_paths, walk):
     opts = ct.TraceOptions(max_bounces=8, russian_roulette=True, nee=True)
     jobs = _jobs(scenes)
@@ -69,10 +77,10 @@ def test_batch_progressive_frames(scenes):
         br.run()
         got = br.images()
         walk = br.info()["walk"]
-    from caustic import _native
+        assert walk == PER_JOB
 
     for job, img in zip(jobs, got):
-        _native.check(job.scene._lib.ct_scene_set_option(job.scene.handle, 1, walk))
+        _force_walk(job.scene, walk)
         four = ct.render_image(job.scene, job.frame, ct.RenderOptions(
             max_bounces=6, russian_roulette=False, nee=True, width=job.width, height=job.height, spp=4,
             seed=job.seed))
@@ -83,6 +91,12 @@ def test_batch_progressive_frames(scenes):
 def test_batch_rejects_bad_jobs(scenes):
     opts = ct.TraceOptions()
     jobs = _jobs(scenes[:1])
+    for walk in (3, -2):
+        with pytest.raises(ct.CausticError, match="batch walk"):
+            ct.BatchRenderer(jobs, opts, walk=walk)
+    bad = [ct.Job(jobs[0].scene, jobs[0].frame, 0, 8, 1)]
     with pytest.raises(ct.CausticError):
-        ct.BatchRenderer(jobs, opts, walk=1)
+        ct.BatchRenderer(bad, opts)
+    with pytest.raises(ct.CausticError, match="wave_paths"):
+        ct.BatchRenderer(jobs, opts, wave_paths=-1)
     jobs[0].scene.close()

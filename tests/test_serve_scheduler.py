@@ -1,0 +1,131 @@
+"""Serving scheduler (host logic) with a fake executor: admission by memory
+budget, progressive chunks, retirement, and the waiting queue."""
+import caustic as ct
+from caustic.serve import PATH_STATE_BYTES, STEPS_IN_FLIGHT, RenderServer, Request
+
+
+class FakeExecutor:
+    def __init__(self, scene_bytes):
+        self.sb = scene_bytes
+        self.steps = []
+        self.live = set()
+        self.peak_live = 0
+
+    def scene_bytes(self, name):
+        return self.sb[name]
+
+    def allocate(self, req):
+        self.live.add(req.rid)
+        self.peak_live = max(self.peak_live, len(self.live))
+        return {"rid": req.rid, "passes": []}
+
+    def launch(self, items):
+        self.steps.append([(r.rid, first, p) for r, _, first, p in items])
+        self.pending = getattr(self, "pending", 0) + 1
+        for r, buf, first, p in items:
+            buf["passes"].append((first, p))
+        return len(self.steps)
+
+    def wait(self, ticket):
+        self.pending -= 1
+        self.waited = getattr(self, "waited", []) + [ticket]
+
+    def fetch(self, req, buf):
+        return buf["passes"]
+
+    def release(self, buf):
+        self.live.discard(buf["rid"])
+
+
+def _req(rid, side, spp, scene="a", arrival=0.0):
+    frame = ct.camera_frame(ct.CORNELL_BOX.camera, 1.0)
+    return Request(rid, scene, frame, side, side, spp, seed=rid, arrival=arrival)
+
+
+class Clock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        self.t += 0.001
+        return self.t
+
+
+def test_every_request_gets_exactly_its_passes_in_order():
+    ex = FakeExecutor({"a": 1000, "b": 2000})
+    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=64 * 64 * 4, clock=Clock())
+    reqs = [_req(0, 64, 10), _req(1, 32, 3, "b"), _req(2, 128, 7), _req(3, 16, 1)]
+    for r in reqs:
+        srv.submit(r)
+    srv.drain()
+    assert sorted(r.request.rid for r in srv.results) == [0, 1, 2, 3]
+    assert ex.waited == sorted(ex.waited) and ex.pending == 0  # steps complete in launch order
+    for res in srv.results:
+        passes = res.image
+        # contiguous progressive chunks covering exactly 0..spp-1
+        k = 0
+        for first, p in passes:
+            assert first == k and p >= 1
+            k += p
+        assert k == res.request.spp
+
+
+def test_admission_respects_the_budget_and_queues_the_rest():
+    ex = FakeExecutor({"a": 10_000})
+    step_paths = 1000
+    buf = 100 * 100 * 12
+    budget = 10_000 + STEPS_IN_FLIGHT * step_paths * PATH_STATE_BYTES + 2 * buf  # room for two 100x100 requests
+    srv = RenderServer(ex, budget_bytes=budget, step_paths=step_paths, clock=Clock())
+    for i in range(6):
+        srv.submit(_req(i, 100, 3))
+    srv.step()
+    assert len(srv.active) + len(srv.results) <= 2 and len(srv.waiting) >= 4
+    while srv.busy():
+        srv.step()
+        assert srv.resident_bytes() <= budget
+    assert ex.peak_live <= 2 and len(srv.results) == 6
+    # arrival order is kept for admission
+    admitted = sorted(srv.results, key=lambda r: r.admitted)
+    assert [r.request.rid for r in admitted] == sorted(r.request.rid for r in admitted)
+
+
+def test_a_request_too_large_for_the_budget_is_rejected():
+    import pytest
+
+    ex = FakeExecutor({"a": 10})
+    srv = RenderServer(ex, budget_bytes=1000, step_paths=1, clock=Clock())
+    srv.submit(_req(0, 100, 1))
+    with pytest.raises(ValueError, match="exceeds the device-memory budget"):
+        srv.step()
+
+
+def test_small_requests_finish_while_a_large_one_continues():
+    ex = FakeExecutor({"a": 0})
+    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=256 * 256, max_passes_per_step=4, clock=Clock())
+    srv.submit(_req(0, 256, 64))
+    srv.step()
+    srv.submit(_req(1, 32, 2))  # arrives while the large request is in flight
+    for _ in range(3):
+        srv.step()
+    done = {r.request.rid for r in srv.results}
+    assert 1 in done and 0 not in done  # continuous batching: joined and left mid-flight
+    assert any(len(items) == 2 for items in ex.steps)  # and shared steps with it
+
+
+def test_steps_are_pipelined_and_bounded():
+    ex = FakeExecutor({"a": 0})
+    step_paths = 64 * 64
+    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=step_paths, min_chunk_paths=0, clock=Clock())
+    for i in range(20):
+        srv.submit(_req(i, 64, 5))
+    srv.step()
+    assert ex.pending == 1  # launched, not waited for
+    srv.step()
+    assert ex.pending == STEPS_IN_FLIGHT - 1
+    srv.drain()
+    # every step holds at most step_paths paths plus one request's chunk
+    for items in ex.steps:
+        assert sum(p * 64 * 64 for _, _, p in items) <= 2 * step_paths
+    # round robin: every request was in the first few steps
+    first = {rid for items in ex.steps[:20] for rid, _, _ in items}
+    assert first == set(range(20))
