@@ -144,6 +144,7 @@ SIGNATURES = {
     "ct_scene_destroy": (None, [P]),
     "ct_scene_device_bytes": (C.c_uint64, [P]),
     "ct_scene_set_option": (C.c_int, [P, C.c_int32, C.c_int64]),
+    "ct_scene_walk": (C.c_int32, [P]),
     "ct_trace_closest": (C.c_int, [P, P, C.c_uint32, P, P, P, P, C.POINTER(ct_stats)]),
     "ct_trace_occluded": (C.c_int, [P, P, C.c_uint32, P, C.POINTER(ct_stats)]),
     "ct_trace_closest_device": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P]),

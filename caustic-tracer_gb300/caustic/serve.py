@@ -65,6 +65,7 @@ class Result:
 @dataclass
 class _Active:
     req: Request
+    seq: int = 0     # admission order
     issued: int = 0  # passes launched
     done: int = 0    # passes completed
     admitted: float = 0.0
@@ -75,6 +76,7 @@ class Executor(Protocol):
     """Device side of the server (a fake one drives the scheduler in tests)."""
 
     def scene_bytes(self, name: str) -> int: ...
+    def walk_class(self, name: str) -> int: ...   # requests of one class share a step
     def allocate(self, req: Request): ...
     def launch(self, items: Sequence[tuple]): ...   # (request, buffer, first pass, passes) -> ticket
     def wait(self, ticket) -> None: ...
@@ -84,7 +86,7 @@ class Executor(Protocol):
 
 class RenderServer:
     def __init__(self, executor: Executor, budget_bytes: int = 120 << 30, step_paths: int = 8 << 20,
-                 min_chunk_paths: int = 1 << 20, max_passes_per_step: Optional[int] = None,
+                 min_chunk_paths: int = 8 << 20, max_passes_per_step: Optional[int] = None,
                  clock: Callable[[], float] = time.perf_counter):
         self.ex = executor
         self.budget = int(budget_bytes)
@@ -100,7 +102,8 @@ class RenderServer:
         self.peak_bytes = 0
         self.steps = 0
         self.samples = 0
-        self._rr = 0  # round-robin start of the next step
+        self._seq = 0
+        self._next = 0  # admission number the next step starts from (round robin)
 
     # -- admission -----------------------------------------------------------
     def _path_bytes(self) -> int:
@@ -123,32 +126,49 @@ class RenderServer:
                 break  # wait for memory; an idle server always admits the head request
             self.waiting.popleft()
             self.scenes_in_use[req.scene] = self.scenes_in_use.get(req.scene, 0) + 1
-            self.active.append(_Active(req, 0, 0, self.clock(), self.ex.allocate(req)))
+            self.active.append(_Active(req, self._seq, 0, 0, self.clock(), self.ex.allocate(req)))
+            self._seq += 1
             self.peak_bytes = max(self.peak_bytes, self.resident_bytes())
 
     # -- scheduling ------------------------------------------------------------
     def _plan(self) -> list:
-        """Requests with passes left, in round-robin order, until the step holds
-        step_paths paths; each gets an equal share of the step, but at least
-        min_chunk_paths (a request's chunk keeps its scene hot in L2 for a
-        while) and at least one pass, at most what it still needs."""
+        """One step: requests with passes left, in round-robin order from where
+        the last step stopped, all of the first one's walk class, packed into
+        at most step_paths paths (one wave). Each gets an equal share of the
+        step, but at least min_chunk_paths (a request's chunk keeps its scene
+        hot in L2 for a while) and at least one pass, at most what it still
+        needs and what still fits; requests that do not fit wait for the next
+        step, which starts at the first of them."""
         pending = [a for a in self.active if a.issued < a.req.spp]
         if not pending:
             return []
-        k = self._rr % len(pending)
+        pending.sort(key=lambda a: a.seq)
+        k = next((i for i, a in enumerate(pending) if a.seq >= self._next), 0)
         pending = pending[k:] + pending[:k]
+        cls = self.ex.walk_class(pending[0].req.scene)
         share = max(self.step_paths / len(pending), min(self.min_chunk, self.step_paths))
-        plan, paths = [], 0
+        room = self.step_paths
+        plan, skipped = [], None
         for a in pending:
-            left = a.req.spp - a.issued
-            p = max(1, min(left, int(share // max(1, a.req.pixels))))
+            if self.ex.walk_class(a.req.scene) != cls:
+                skipped = a if skipped is None else skipped
+                continue
+            px = max(1, a.req.pixels)
+            want = max(1, min(a.req.spp - a.issued, int(share // px)))
             if self.max_passes:
-                p = min(p, self.max_passes)
+                want = min(want, self.max_passes)
+            fit = room // px
+            if fit == 0 and plan:
+                skipped = a if skipped is None else skipped
+                continue
+            p = max(1, min(want, fit))  # a pass larger than a whole step goes alone (split by pixels)
             plan.append((a, p))
-            paths += p * a.req.pixels
-            if paths >= self.step_paths:
+            room -= p * px
+            if room <= 0:
                 break
-        self._rr += len(plan)
+        last = plan[-1][0]
+        after = [a for a in pending if a.seq > last.seq]
+        self._next = skipped.seq if skipped is not None else (after[0].seq if after else 0)
         return plan
 
     def _complete_oldest(self) -> int:
@@ -242,9 +262,14 @@ class GpuExecutor:
         self.copy_stream = torch.cuda.Stream()
         self._topts = _abi.ct_trace_options(opts.max_bounces, int(opts.russian_roulette), int(opts.nee))
         self._bytes = {k: v.device_bytes for k, v in scenes.items()}
+        self._walk = {k: v.walk for k, v in scenes.items()}
 
     def scene_bytes(self, name: str) -> int:
         return self._bytes[name]
+
+    def walk_class(self, name: str) -> int:
+        # ct_batch gives each trace walk waves of its own: a step of one walk is one wave
+        return self._walk[name]
 
     def allocate(self, req: Request):
         import torch

@@ -69,6 +69,12 @@ class DeviceScene:
     def device_bytes(self) -> int:
         return int(self._lib.ct_scene_device_bytes(self.handle))
 
+    @property
+    def walk(self) -> int:
+        """Trace walk the integrator uses for this scene (0 ordered, 1 ordered
+        with persistent refill, 2 stackless skip-link)."""
+        return int(self._lib.ct_scene_walk(self.handle))
+
     def close(self) -> None:
         if getattr(self, "handle", None):
             self._lib.ct_scene_destroy(self.handle)

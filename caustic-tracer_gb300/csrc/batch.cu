@@ -2,8 +2,8 @@
 //
 // A batch is a list of jobs (scene, camera, size, frame indices, passes, sum
 // buffer). Their paths are packed into waves of up to `wave_paths` paths. The
-// planner takes the jobs grouped by trace walk and then by scene (a wave runs
-// one walk's kernel; the paths in flight at any time touch few BVHs) and
+// planner takes the jobs grouped by trace walk and then by scene (a wave
+// runs one walk's kernel; the paths in flight at any time touch few BVHs) and
 // appends each job's passes as chunks: as many whole passes as fit in the
 // open wave, laid out pass-major; a pass larger than a wave is split by pixel
 // ranges over several waves. A wave holds at most one chunk of any job, so
@@ -64,7 +64,10 @@ int job_walk(const ct_batch* b, uint32_t j) {
 
 void plan(ct_batch* b, uint64_t cap) {
   const uint32_t n = (uint32_t)b->jobs.size();
-  // Jobs grouped by walk, then by scene (groups in order of first appearance).
+  // Jobs grouped by walk, then by scene (groups in order of first
+  // appearance); a wave holds jobs of one walk and runs its kernel. (The two
+  // ordered walks give the same hits, but a wave of shallow and deep trees
+  // together runs slower under either kernel than the two apart.)
   std::vector<uint32_t> order(n), group(n);
   std::vector<int> walk(n);
   std::unordered_map<const ct_scene*, uint32_t> first_job;

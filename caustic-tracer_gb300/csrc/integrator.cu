@@ -136,6 +136,8 @@ int integrator_walk_form(const ct_scene* s) { return walk_form(s); }
 
 extern "C" {
 
+int32_t ct_scene_walk(const ct_scene* scene) { return scene ? ct::walk_form(scene) : -1; }
+
 ct_status ct_accumulate_passes_device(ct_scene* scene, const ct_camera_frame* frame, int32_t width, int32_t height,
                                       uint32_t first_frame_index, int32_t passes, const ct_trace_options* opts,
                                       float* accum, float* sumsq, void* stream) {

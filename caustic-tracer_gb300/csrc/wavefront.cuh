@@ -195,14 +195,20 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
 //                   walks finish (pays off for deep trees);
 //   kWalkSkip       the reference's stackless skip-link walk (no stack; all
 //                   lanes visit nodes in the same order; for small trees);
-//   kWalkPerJob     BATCH only, a planning mode: every wave holds jobs of one
-//                   walk, the one each job's scene uses alone, and runs that
-//                   walk's kernel.
+//   kWalkPerJob     BATCH only, a planning mode: each job walks as its scene
+//                   does alone; a wave holds jobs of one walk and runs its
+//                   kernel.
 enum WalkForm : int { kWalkThread = 0, kWalkPersistent = 1, kWalkSkip = 2, kWalkPerJob = 3 };
 
 // Closest hits of the bounce-b path queue plus the shadow rays of bounce b-1.
+// The ordered walks are latency-bound chains of dependent node loads, so they
+// are held to 32 registers (16 blocks = 2048 threads per SM); the skip-link
+// walk (small trees, short walks) keeps its registers.
+template <int FORM>
+constexpr int trace_min_blocks() { return FORM == 2 ? 8 : 16; }
+
 template <int FORM, bool BATCH>
-__global__ void __launch_bounds__(kBlock, 8) k_trace(WaveArgs a, int32_t bounce) {
+__global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(WaveArgs a, int32_t bounce) {
   const uint32_t n_ext = bounce <= a.max_bounces ? a.counts[bounce] : 0u;
   const uint32_t n_sh = bounce > 0 ? a.counts[a.max_bounces + 2 + bounce - 1] : 0u;
   uint32_t fallbacks = 0;

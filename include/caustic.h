@@ -208,6 +208,10 @@ uint64_t ct_scene_device_bytes(const ct_scene* scene);
 #define CT_OPT_WALK 1
 #define CT_OPT_WAVE_PATHS 2
 ct_status ct_scene_set_option(ct_scene* scene, int32_t option, int64_t value);
+/* Trace walk the integrator uses for the scene (0, 1 or 2 as above: the
+ * CT_OPT_WALK value, or the choice from the tree); -1 for a NULL scene. A
+ * scheduler groups jobs by it (ct_batch gives each walk waves of its own). */
+int32_t ct_scene_walk(const ct_scene* scene);
 
 /* ---- ray queries --------------------------------------------------------
  * intersectClosest (intersect.ts:202-282) over a batch of rays. rays holds

@@ -14,6 +14,9 @@ class FakeExecutor:
     def scene_bytes(self, name):
         return self.sb[name]
 
+    def walk_class(self, name):
+        return 1 if name.startswith("skip") else 0
+
     def allocate(self, req):
         self.live.add(req.rid)
         self.peak_live = max(self.peak_live, len(self.live))
@@ -101,7 +104,7 @@ def test_a_request_too_large_for_the_budget_is_rejected():
 
 def test_small_requests_finish_while_a_large_one_continues():
     ex = FakeExecutor({"a": 0})
-    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=256 * 256, max_passes_per_step=4, clock=Clock())
+    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=4 * 256 * 256, max_passes_per_step=2, clock=Clock())
     srv.submit(_req(0, 256, 64))
     srv.step()
     srv.submit(_req(1, 32, 2))  # arrives while the large request is in flight
@@ -123,9 +126,31 @@ def test_steps_are_pipelined_and_bounded():
     srv.step()
     assert ex.pending == STEPS_IN_FLIGHT - 1
     srv.drain()
-    # every step holds at most step_paths paths plus one request's chunk
+    # every step fits in step_paths paths (one wave)
     for items in ex.steps:
-        assert sum(p * 64 * 64 for _, _, p in items) <= 2 * step_paths
+        assert sum(p * 64 * 64 for _, _, p in items) <= step_paths
     # round robin: every request was in the first few steps
     first = {rid for items in ex.steps[:20] for rid, _, _ in items}
     assert first == set(range(20))
+
+
+def test_steps_fill_one_wave_and_never_mix_walk_classes():
+    ex = FakeExecutor({"a": 0, "skip": 0})
+    step_paths = 100_000
+    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=step_paths, min_chunk_paths=30_000, clock=Clock())
+    sides = [64, 200, 128, 300, 16, 90, 250, 40]
+    for i, side in enumerate(sides):
+        srv.submit(_req(i, side, 7, "skip" if i % 3 == 0 else "a"))
+    srv.submit(_req(99, 400, 2))  # one pass (160,000 paths) is larger than a step
+    srv.drain()
+    side_of = {i: side for i, side in enumerate(sides)}
+    side_of[99] = 400
+    cls = {i: (1 if i % 3 == 0 else 0) for i in range(len(sides))}
+    cls[99] = 0
+    for items in ex.steps:
+        paths = sum(p * side_of[rid] ** 2 for rid, _, p in items)
+        assert paths <= step_paths or (len(items) == 1 and items[0][2] == 1)
+        assert len({cls[rid] for rid, _, _ in items}) == 1
+    assert sorted(r.request.rid for r in srv.results) == sorted(list(range(len(sides))) + [99])
+    for res in srv.results:
+        assert sum(p for _, p in res.image) == res.request.spp
