@@ -130,3 +130,4 @@ def test_ragged_batch_sizes(oracle, random_scene):
         assert len(hits.prim) == n
         if n:
             check_closest(oracle, packed, rays_all[:n], hits, f"n={n}")
+
