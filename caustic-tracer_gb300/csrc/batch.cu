@@ -183,7 +183,7 @@ ct_status create(const ct_batch_job* jobs, uint32_t count, const ct_trace_option
     CT_CHECK_ARG(j.scene->device == device, "job %u: scene lives on device %d, job 0 on %d", i, j.scene->device, device);
     CT_CHECK_ARG(j.passes >= 0, "job %u: passes %d is negative", i, j.passes);
     if (walk == 0 || walk == 1)
-      CT_CHECK_ARG(j.scene->depth <= ctk::kStackSize, "job %u: tree too deep for the ordered walk", i);
+      CT_CHECK_ARG(j.scene->stack_need <= ctk::kStackSize, "job %u: tree too deep for the ordered walk", i);
     ct_status st = check_options(&j.frame, j.width, j.height, o->max_bounces);
     if (st != CT_OK) return fail(st, "job %u: %s", i, last_error());
   }

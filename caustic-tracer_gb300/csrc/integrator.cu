@@ -22,10 +22,11 @@ constexpr uint32_t kPersistentDepth = 16;      // tree depth above which traces 
 constexpr uint32_t kSkipMaxNodes = 31;         // trees this small use the stackless skip-link walk
 
 // Walk form of a scene's trace launches: the scene's CT_OPT_WALK when set,
-// else by tree size and depth.
+// else by tree size and depth (the stackless walk for small trees and for
+// trees whose ordered walk could outgrow its stack).
 int walk_form(const ct_scene* s) {
   if (s->opt_walk >= 0) return s->opt_walk;
-  if (s->node_count <= kSkipMaxNodes) return kWalkSkip;
+  if (s->node_count <= kSkipMaxNodes || s->stack_need > ctk::kStackSize) return kWalkSkip;
   return s->depth > kPersistentDepth ? kWalkPersistent : kWalkThread;
 }
 

@@ -4,11 +4,14 @@
 // ranges, light and material indices) before anything reaches the device,
 // so a malformed array is rejected with CT_ERR_INVALID_ARGUMENT instead of
 // becoming an out-of-bounds read. It also derives the traversal layout the
-// kernels use: one 64-byte record per interior node holding both children's
-// boxes interleaved by axis plus the two child references, so a traversal
-// step is a single coalesced load instead of two dependent node loads.
+// ordered walk uses: the binary tree collapsed into 4-wide records of 128
+// bytes (four child boxes by axis plus four child references), so one step
+// of the walk tests four boxes with one cache line of loads and a ray takes
+// about half the dependent steps of the binary walk.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <new>
 #include <vector>
 
@@ -99,14 +102,12 @@ bool is_index(float f, uint32_t limit) {
 }
 
 // Structural check of the skip-link array (bvh.ts:319-381 invariants that the
-// traversals rely on) plus depth and the interior-record numbering.
-ct_status check_tree(const ct_packed_scene_view& v, std::vector<int32_t>& pair_of,
-                     uint32_t* interior_count, uint32_t* depth_out) {
+// traversals rely on) plus the depth and the number of interior nodes.
+ct_status check_tree(const ct_packed_scene_view& v, uint32_t* interior_count, uint32_t* depth_out) {
   const float* n = v.nodes;
   const uint32_t N = v.node_count;
   for (size_t i = 0; i < (size_t)N * CT_NODE_STRIDE; i++)
     if (!std::isfinite(n[i])) return fail(CT_ERR_INVALID_ARGUMENT, "nodes[%zu] is not finite", i);
-  pair_of.assign(N, -1);
   uint32_t interior = 0, depth = 0;
   // Explicit post-order walk: frame = (node, depth, stage, end of left subtree).
   struct F {
@@ -133,7 +134,7 @@ ct_status check_tree(const ct_packed_scene_view& v, std::vector<int32_t>& pair_o
         st.pop_back();
         continue;
       }
-      pair_of[f.node] = (int32_t)interior++;
+      interior++;
       f.stage = 1;
       const uint32_t child = f.node + 1, d = f.depth + 1;
       st.push_back({child, d, 0, 0});
@@ -157,10 +158,94 @@ ct_status check_tree(const ct_packed_scene_view& v, std::vector<int32_t>& pair_o
   return CT_OK;
 }
 
-int32_t child_ref(const float* n, const std::vector<int32_t>& pair_of, uint32_t child) {
-  const float* r = n + (size_t)child * CT_NODE_STRIDE;
-  if (r[7] >= 0.0f) return ~(int32_t)(uint32_t)r[7];
-  return pair_of[child];
+// Collapses the reference's binary tree (bvh.ts node array) into the 4-wide
+// records the ordered walk traverses: a record starts from a binary interior
+// node and opens its largest-area interior child until it holds four children
+// or only leaves. Record layout, 8 float4 = 128 bytes (one cache line):
+//   [0] lo.x  [1] hi.x  [2] lo.y  [3] hi.y  [4] lo.z  [5] hi.z   (children 0..3)
+//   [6] child references: >= 0 record, < 0 ~leafword            [7] unused
+// Empty slots hold NaN bounds, which no box test accepts. The child boxes are
+// the reference's own node boxes, so every box the walk tests is one the
+// reference tests. *stack_need is the deepest stack the ordered walk can
+// build: along the worst root-to-leaf path, each record pushes all but one
+// of its children.
+void build_quads(const ct_packed_scene_view& v, std::vector<float4>& recs, int32_t* root_ref,
+                 uint32_t* stack_need) {
+  const float* n = v.nodes;
+  auto node = [&](uint32_t i) { return n + (size_t)i * CT_NODE_STRIDE; };
+  auto leaf = [&](uint32_t i) { return node(i)[7] >= 0.0f; };
+  auto right = [&](uint32_t i) { return (uint32_t)node(i + 1)[3]; };  // the left child's skip link
+  auto area = [&](uint32_t i) {
+    const float* r = node(i);
+    const double dx = (double)r[4] - r[0], dy = (double)r[5] - r[1], dz = (double)r[6] - r[2];
+    return dx * dy + dy * dz + dz * dx;
+  };
+  recs.assign(8, make_float4(0, 0, 0, 0));
+  *stack_need = 0;
+  if (v.node_count == 0 || leaf(0)) {
+    *root_ref = v.node_count ? ~(int32_t)(uint32_t)node(0)[7] : ~0;
+    return;
+  }
+  *root_ref = 0;
+  std::vector<uint32_t> kids_of;       // per record: up to 4 binary child nodes
+  std::vector<uint8_t> count_of;       // per record: children
+  std::vector<std::pair<uint32_t, uint32_t>> todo{{0u, 0u}};  // (binary interior node, record)
+  kids_of.assign(4, 0);
+  count_of.assign(1, 0);
+  while (!todo.empty()) {
+    const auto [b, r] = todo.back();
+    todo.pop_back();
+    uint32_t kids[4] = {b + 1, right(b), 0, 0};
+    int k = 2;
+    while (k < 4) {
+      int best = -1;
+      double best_area = -1.0;
+      for (int c = 0; c < k; c++)
+        if (!leaf(kids[c]) && area(kids[c]) > best_area) best = c, best_area = area(kids[c]);
+      if (best < 0) break;
+      const uint32_t x = kids[best];
+      kids[best] = x + 1;
+      kids[k++] = right(x);
+    }
+    const float nan = std::numeric_limits<float>::quiet_NaN();
+    float lo[3][4], hi[3][4];
+    int32_t refs[4] = {0, 0, 0, 0};
+    for (int c = 0; c < 4; c++) {
+      for (int a = 0; a < 3; a++) lo[a][c] = hi[a][c] = nan;
+      if (c >= k) continue;
+      const float* cn = node(kids[c]);
+      for (int a = 0; a < 3; a++) lo[a][c] = cn[a], hi[a][c] = cn[4 + a];
+      if (leaf(kids[c])) {
+        refs[c] = ~(int32_t)(uint32_t)cn[7];
+      } else {
+        const uint32_t child = (uint32_t)(recs.size() / 8);
+        recs.resize(recs.size() + 8, make_float4(0, 0, 0, 0));
+        count_of.push_back(0);
+        refs[c] = (int32_t)child;
+        todo.push_back({kids[c], child});
+      }
+    }
+    float4* q = &recs[(size_t)r * 8];
+    for (int a = 0; a < 3; a++) {
+      q[2 * a] = make_float4(lo[a][0], lo[a][1], lo[a][2], lo[a][3]);
+      q[2 * a + 1] = make_float4(hi[a][0], hi[a][1], hi[a][2], hi[a][3]);
+    }
+    std::memcpy(&q[6], refs, sizeof refs);
+    count_of[r] = (uint8_t)k;
+  }
+  // Children are numbered after their parents: one backward sweep gives the
+  // worst stack below each record.
+  const size_t R = recs.size() / 8;
+  std::vector<uint32_t> need(R, 0);
+  for (size_t r = R; r-- > 0;) {
+    int32_t refs[4];
+    std::memcpy(refs, &recs[r * 8 + 6], sizeof refs);
+    uint32_t below = 0;
+    for (int c = 0; c < count_of[r]; c++)
+      if (refs[c] >= 0) below = std::max(below, need[(size_t)refs[c]]);
+    need[r] = (uint32_t)(count_of[r] - 1) + below;
+  }
+  *stack_need = need[0];
 }
 
 ct_status validate_view(const ct_packed_scene_view& v) {
@@ -211,7 +296,7 @@ void destroy(ct_scene* s) {
   cudaGetDevice(&prev);
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
-  for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->pairs, &s->mats, &s->lights, &s->prim_object, &s->io,
+  for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->quads, &s->mats, &s->lights, &s->prim_object, &s->io,
                           &s->counters})
     b->release(&s->device_bytes);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -225,26 +310,18 @@ void destroy(ct_scene* s) {
 ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   ct_status st = validate_view(v);
   if (st != CT_OK) return st;
-  std::vector<int32_t> pair_of;
   uint32_t interior = 0, depth = 0;
   if (v.node_count > 0) {
-    st = check_tree(v, pair_of, &interior, &depth);
+    st = check_tree(v, &interior, &depth);
     if (st != CT_OK) return st;
   }
-  std::vector<float4> pairs((size_t)(interior > 0 ? interior : 1) * 4, make_float4(0, 0, 0, 0));
-  for (uint32_t i = 0; i < v.node_count; i++) {
-    const int32_t p = pair_of[i];
-    if (p < 0) continue;
-    const uint32_t left = i + 1, right = (uint32_t)v.nodes[(size_t)left * CT_NODE_STRIDE + 3];
-    const float* L = v.nodes + (size_t)left * CT_NODE_STRIDE;
-    const float* R = v.nodes + (size_t)right * CT_NODE_STRIDE;
-    float4* rec = &pairs[(size_t)p * 4];
-    rec[0] = make_float4(L[0], L[4], L[1], L[5]);
-    rec[1] = make_float4(R[0], R[4], R[1], R[5]);
-    rec[2] = make_float4(L[2], L[6], R[2], R[6]);
-    const int32_t cl = child_ref(v.nodes, pair_of, left), cr = child_ref(v.nodes, pair_of, right);
-    int32_t refs[4] = {cl, cr, 0, 0};
-    std::memcpy(&rec[3], refs, sizeof refs);
+  std::vector<float4> quads;
+  int32_t root_ref = ~0;
+  uint32_t stack_need = 0;
+  try {
+    build_quads(v, quads, &root_ref, &stack_need);
+  } catch (const std::bad_alloc&) {
+    return fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");
   }
 
   ct_scene* s = new (std::nothrow) ct_scene();
@@ -270,10 +347,11 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   s->mat_count = v.mat_count;
   s->light_count = v.light_count;
   s->depth = depth;
+  s->stack_need = stack_need;
   s->sky = v.sky;
   if ((st = upload(s, s->prims, reinterpret_cast<const float4*>(v.prims), (size_t)v.prim_count * 4, 4)) != CT_OK ||
       (st = upload(s, s->nodes, reinterpret_cast<const float4*>(v.nodes), (size_t)v.node_count * 2, 2)) != CT_OK ||
-      (st = upload(s, s->pairs, pairs.data(), pairs.size(), 4)) != CT_OK ||
+      (st = upload(s, s->quads, quads.data(), quads.size(), 8)) != CT_OK ||
       (st = upload(s, s->mats, reinterpret_cast<const float4*>(v.mats), (size_t)v.mat_count * 4, 4)) != CT_OK ||
       (st = upload(s, s->lights, v.lights, v.light_count, 1)) != CT_OK ||
       (st = upload(s, s->prim_object, v.prim_object, v.prim_count, 1)) != CT_OK ||
@@ -292,14 +370,14 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   ctk::SceneDev& d = s->dev;
   d.prims = s->prims.as<float4>();
   d.nodes = s->nodes.as<float4>();
-  d.pairs = s->pairs.as<float4>();
+  d.quads = s->quads.as<float4>();
   d.mats = s->mats.as<float4>();
   d.lights = s->lights.as<int32_t>();
   d.prim_object = s->prim_object.as<uint32_t>();
   d.node_count = v.node_count;
   d.light_count = v.light_count;
   if (v.node_count > 0) {
-    d.root_ref = v.nodes[7] >= 0.0f ? ~(int32_t)(uint32_t)v.nodes[7] : pair_of[0];
+    d.root_ref = root_ref;
     for (int k = 0; k < 3; k++) {
       d.root_lo[k] = v.nodes[k];
       d.root_hi[k] = v.nodes[4 + k];
@@ -339,7 +417,8 @@ ct_status ct_scene_set_option(ct_scene* scene, int32_t option, int64_t value) {
     case CT_OPT_WALK:
       CT_CHECK_ARG(value >= -1 && value <= 2, "CT_OPT_WALK %lld outside [-1, 2]", (long long)value);
       if (value == 0 || value == 1)
-        CT_CHECK_ARG(scene->depth <= ctk::kStackSize, "tree depth %u exceeds the ordered walk's stack", scene->depth);
+        CT_CHECK_ARG(scene->stack_need <= ctk::kStackSize, "the ordered walk of this tree needs %u stack entries (%d)",
+                     scene->stack_need, ctk::kStackSize);
       scene->opt_walk = (int32_t)value;
       return CT_OK;
     case CT_OPT_WAVE_PATHS:

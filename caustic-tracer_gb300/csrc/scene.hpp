@@ -52,10 +52,11 @@ struct ct_scene {
   cudaStream_t stream = nullptr;
   std::mutex lock;
 
-  // Device copies of the packed arrays plus the interior pair records.
-  ct::DeviceBuffer prims, nodes, pairs, mats, lights, prim_object;
+  // Device copies of the packed arrays plus the 4-wide walk records.
+  ct::DeviceBuffer prims, nodes, quads, mats, lights, prim_object;
   uint32_t prim_count = 0, node_count = 0, interior_count = 0, mat_count = 0, light_count = 0;
-  uint32_t depth = 0;  // deepest root-to-leaf path, in nodes
+  uint32_t depth = 0;       // deepest root-to-leaf path, in nodes
+  uint32_t stack_need = 0;  // deepest stack the ordered walk can build
   ct_sky sky{};
   ctk::SceneDev dev{};
 

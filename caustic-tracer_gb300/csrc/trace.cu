@@ -18,11 +18,12 @@ namespace {
 
 std::atomic<int32_t> g_variant{0};  // 0 ordered short-stack walk, 1 stackless skip links
 
-// 16 blocks of 128 per SM (32 registers, a few spilled): the walk is a chain
-// of dependent loads and gains more from warps in flight than it loses to
-// the spills (580 -> 646 Mrays/s on the 1M-triangle soup against 8 blocks).
+// 12 blocks of 128 per SM (40 registers, a few spilled): the walk is a chain
+// of dependent loads and gains more from warps in flight than it loses to the
+// spills (1M-triangle soup: 683 Mrays/s, against 580 at 8 blocks and 614 at
+// 16, where the four-box step spills heavily).
 template <int VARIANT, bool ANY>
-__global__ void __launch_bounds__(128, 16) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
+__global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
                                                uint32_t n, int32_t* __restrict__ prim,
                                                float* __restrict__ t_out, float* __restrict__ u_out,
                                                float* __restrict__ v_out,
@@ -112,8 +113,8 @@ template <bool ANY>
 ct_status launch(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, float* t, float* u,
                  float* v, uint8_t* blocked, cudaStream_t stream) {
   if (n == 0) return CT_OK;
-  // A tree deeper than the ordered walk's stack uses the stackless walk.
-  const int variant = (g_variant.load() == 1 || s->depth > ctk::kStackSize) ? 1 : 0;
+  // A tree whose walk could outgrow the ordered walk's stack uses the stackless walk.
+  const int variant = (g_variant.load() == 1 || s->stack_need > ctk::kStackSize) ? 1 : 0;
   const float4* r4 = reinterpret_cast<const float4*>(rays);
   uint32_t* cnt = s->counters.as<uint32_t>();
   CT_CUDA(cudaMemsetAsync(cnt + kCountQueue, 0, sizeof(uint32_t), stream));  // persistent work counter
@@ -192,7 +193,7 @@ ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, 
   uint32_t counters[2] = {0, 0};
   CT_CUDA(cudaMemcpyAsync(counters, s->counters.ptr, sizeof counters, cudaMemcpyDeviceToHost, stream));
   CT_CUDA(cudaStreamSynchronize(stream));
-  if (counters[1]) return fail(CT_ERR_UNSUPPORTED, "traversal stack overflow (tree depth %u)", s->depth);
+  if (counters[1]) return fail(CT_ERR_UNSUPPORTED, "traversal stack overflow (stack need %u)", s->stack_need);
   if (stats) {
     float k_ms = 0, all_ms = 0;
     cudaEventElapsedTime(&k_ms, s->ev1, s->ev2);

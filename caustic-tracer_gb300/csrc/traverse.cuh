@@ -21,7 +21,7 @@
 
 namespace ctk {
 
-constexpr int kStackSize = 64;               // ordered-walk stack (tree depth is checked on upload)
+constexpr int kStackSize = 64;               // ordered-walk stack (the tree's need is computed on upload)
 constexpr float kEps = 5.9604645e-8f;        // 2^-24
 constexpr float kErrK = 16.0f * kEps;        // error-bound multiplier (2x the first-order bound)
 // Max relative error of a reported float32 t, checked against the first-order
@@ -29,13 +29,14 @@ constexpr float kErrK = 16.0f * kEps;        // error-bound multiplier (2x the f
 constexpr float kTRel = 4e-6f;
 constexpr float kBoxWiden = 1.0000005f;      // 1 + 2*gamma(3), rounded up
 
-// Device view of a scene. `pairs` holds one 64-byte record per interior node
-// of the reference BVH: the boxes of both children interleaved by axis and
-// the two child references (>= 0 interior record, < 0 ~leafword).
+// Device view of a scene. `quads` holds the reference BVH collapsed to four
+// children per record (128 bytes): lo.x, hi.x, lo.y, hi.y, lo.z, hi.z of the
+// four children (one float4 each; NaN for an empty slot), then the four child
+// references (>= 0 record, < 0 ~leafword).
 struct SceneDev {
   const float4* __restrict__ prims;  // 4 per primitive (pack.ts:6-10)
   const float4* __restrict__ nodes;  // 2 per reference node (bvh.ts:6-15)
-  const float4* __restrict__ pairs;  // 4 per interior node
+  const float4* __restrict__ quads;  // 8 per 4-wide record
   const float4* __restrict__ mats;   // 4 per material (pack.ts:12-16)
   const int32_t* __restrict__ lights;
   const uint32_t* __restrict__ prim_object;
@@ -422,13 +423,14 @@ __device__ __forceinline__ float box_entry(const RayF& r, float lox, float hix, 
 // Upper bound of the reference's current closest distance (prunes boxes).
 __device__ __forceinline__ float prune_bound(const HitF& h) { return h.t + h.err; }
 
-// Ordered front-to-back walk over the interior pair records (the reference's
-// intersectClosest, intersect.ts:202-282; with `any`, the any-hit query of
-// occluded, intersect.ts:368-420), as a state machine advanced one step at a
-// time: a step expands one interior record (both child boxes, nearer child
-// first, farther child pushed with its entry distance), tests one primitive of
-// the current leaf, or pops the stack past entries beyond the closest hit.
-// Equal-cost steps keep the lanes of a warp in step with each other.
+// Ordered front-to-back walk over the 4-wide records (the reference's
+// intersectClosest, intersect.ts:202-282, on the same boxes with two binary
+// levels per step; with `any`, the any-hit query of occluded,
+// intersect.ts:368-420), as a state machine advanced one step at a time: a
+// step expands one record (four child boxes; the nearest child entered, the
+// others pushed farthest first with their entry distances), tests one
+// primitive of the current leaf, or pops the stack past entries beyond the
+// closest hit. Equal-cost steps keep the lanes of a warp in step.
 struct Walk {
   RayF r;
   HitF h;
@@ -481,26 +483,42 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
     }
     if (++w.cur == w.end) w.ref = kWalkPop;
   } else if (w.ref >= 0 && w.ref != kWalkPop) {
-    const float4* pr = s.pairs + (size_t)w.ref * 4;
-    const float4 n0 = __ldg(pr), n1 = __ldg(pr + 1), n2 = __ldg(pr + 2), n3 = __ldg(pr + 3);
+    const float4* q = s.quads + (size_t)w.ref * 8;
+    const float4 xl = __ldg(q), xh = __ldg(q + 1), yl = __ldg(q + 2), yh = __ldg(q + 3);
+    const float4 zl = __ldg(q + 4), zh = __ldg(q + 5);
+    const int4 c4 = __ldg(reinterpret_cast<const int4*>(q + 6));
     const float bound = prune_bound(w.h);
-    const float tl = box_entry(w.r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, bound);
-    const float tr = box_entry(w.r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, bound);
-    const int32_t cl = __float_as_int(n3.x), cr = __float_as_int(n3.y);
-    if (tl != INFINITY && tr != INFINITY) {
-      if (w.sp >= kStackSize) {
-        w.overflow = true;
-        w.ref = kWalkDone;
-        return;
+    float t0 = box_entry(w.r, xl.x, xh.x, yl.x, yh.x, zl.x, zh.x, bound);
+    float t1 = box_entry(w.r, xl.y, xh.y, yl.y, yh.y, zl.y, zh.y, bound);
+    float t2 = box_entry(w.r, xl.z, xh.z, yl.z, yh.z, zl.z, zh.z, bound);
+    float t3 = box_entry(w.r, xl.w, xh.w, yl.w, yh.w, zl.w, zh.w, bound);
+    int32_t c0 = c4.x, c1 = c4.y, c2 = c4.z, c3 = c4.w;
+    // Nearest first (misses, +inf, last): a five-exchange sorting network.
+    auto order = [](float& ta, int32_t& ca, float& tb, int32_t& cb) {
+      if (tb < ta) {
+        const float t = ta;
+        ta = tb, tb = t;
+        const int32_t c = ca;
+        ca = cb, cb = c;
       }
-      const bool left_first = tl <= tr;
-      w.stack_ref[w.sp] = left_first ? cr : cl;
-      w.stack_t[w.sp++] = left_first ? tr : tl;
-      walk_enter(w, left_first ? cl : cr);
-    } else if (tl != INFINITY || tr != INFINITY) {
-      walk_enter(w, tl != INFINITY ? cl : cr);
-    } else {
+    };
+    order(t0, c0, t1, c1);
+    order(t2, c2, t3, c3);
+    order(t0, c0, t2, c2);
+    order(t1, c1, t3, c3);
+    order(t1, c1, t2, c2);
+    const int hits = (t0 != INFINITY) + (t1 != INFINITY) + (t2 != INFINITY) + (t3 != INFINITY);
+    if (hits == 0) {
       w.ref = kWalkPop;
+    } else if (w.sp + hits - 1 > kStackSize) {
+      w.overflow = true;
+      w.ref = kWalkDone;
+      return;
+    } else {
+      if (hits > 3) w.stack_ref[w.sp] = c3, w.stack_t[w.sp++] = t3;
+      if (hits > 2) w.stack_ref[w.sp] = c2, w.stack_t[w.sp++] = t2;
+      if (hits > 1) w.stack_ref[w.sp] = c1, w.stack_t[w.sp++] = t1;
+      walk_enter(w, c0);
     }
   }
   if (w.ref == kWalkPop) {

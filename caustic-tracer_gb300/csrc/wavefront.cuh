@@ -201,11 +201,12 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
 enum WalkForm : int { kWalkThread = 0, kWalkPersistent = 1, kWalkSkip = 2, kWalkPerJob = 3 };
 
 // Closest hits of the bounce-b path queue plus the shadow rays of bounce b-1.
-// The ordered walks are latency-bound chains of dependent node loads, so they
-// are held to 32 registers (16 blocks = 2048 threads per SM); the skip-link
-// walk (small trees, short walks) keeps its registers.
+// The ordered walks are latency-bound chains of dependent record loads, so
+// they are held to 40 registers (12 blocks = 1536 threads per SM; 32 registers
+// spill the four-box step and run slower, 64 halve the warps in flight); the
+// skip-link walk (small trees, short walks) keeps its registers.
 template <int FORM>
-constexpr int trace_min_blocks() { return FORM == 2 ? 8 : 16; }
+constexpr int trace_min_blocks() { return FORM == 2 ? 8 : 12; }
 
 template <int FORM, bool BATCH>
 __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(WaveArgs a, int32_t bounce) {
