@@ -14,7 +14,9 @@ from .scene import (CameraSettings, CheckerTexture, Dielectric, Emissive, Lamber
 from .scenes import (CORNELL_BOX, batch_scene, batch_workload, caustic_scene, cornell_box, cornell_unit_box,
                      furnace_scene, random_test_scene, soup_rays, triangle_soup)
 from .batch import BatchRenderer, Job
-from .tonemap import decode_ppm, encode_ppm, tonemap_buffer
-from .tracer import (DEFAULT_TRACE_OPTIONS, T_MIN, DeviceScene, Hits, RenderOptions, TraceOptions,
-                     accumulate_pass, intersect_closest, make_rays, occluded, render_image, set_traversal)
+from .tonemap import decode_ppm, encode_ppm, ppm_device, tonemap_buffer, tonemap_device
+from .tracer import (DEFAULT_TRACE_OPTIONS, T_MIN, DeviceScene, Hits, PickResult, RenderOptions, TraceOptions,
+                     accumulate_pass, intersect_closest, make_rays, occluded, pick, pick_many, render_image,
+                     set_traversal)
+from .serve import RenderServer, Request
 from ._native import CausticError, NativeLibraryError

@@ -167,6 +167,10 @@ SIGNATURES = {
     "ct_batch_destroy": (None, [P]),
     "ct_accumulate_pass_noalloc": (C.c_int, [P, C.POINTER(ct_camera_frame), C.c_int32, C.c_int32, C.c_uint32,
                                              C.POINTER(ct_trace_options), P, P]),
+    "ct_tonemap_device": (C.c_int, [P, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32, P, P]),
+    "ct_ppm_device": (C.c_int, [P, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32, P, C.c_uint64,
+                                C.POINTER(C.c_uint64), P]),
+    "ct_pick": (C.c_int, [P, C.POINTER(ct_camera_frame), C.c_uint32, P, P, P, P, P, P]),
     "ct_profile_enable": (None, [C.c_int32]),
     "ct_profile_reset": (None, []),
     "ct_profile_read": (C.c_int32, [C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_int32]),

@@ -1,4 +1,9 @@
-"""Display transforms (tonemap.ts) and binary PPM (ppm.ts), on the host."""
+"""Display transforms (tonemap.ts) and binary PPM (ppm.ts).
+
+`tonemap_device` / `ppm_device` run the transform on the GPU
+(ct_tonemap_device / ct_ppm_device) on a device sum buffer; the numpy forms
+below serve host arrays (the reference's own helpers run on the host too).
+"""
 from __future__ import annotations
 
 import math
@@ -77,3 +82,44 @@ def decode_ppm(data: bytes):
     if len(rgb) != w * h * 3:
         raise ValueError("truncated PPM data")
     return w, h, rgb
+
+
+MODES = {"aces": 0, "reinhard": 1}
+
+
+def tonemap_device(accum, width: int, height: int, samples: float, exposure_ev: float = 0.0, mode: str = "aces",
+                   stream=None):
+    """tonemapBuffer on the GPU: `accum` is a CUDA float32 tensor of width*height*3
+    sums; returns a CUDA uint8 tensor of width*height*4 RGBA bytes (equal to
+    tonemap_buffer's)."""
+    import ctypes as C
+
+    import torch
+
+    from . import _native
+
+    lib = _native.lib()
+    out = torch.empty(width * height * 4, dtype=torch.uint8, device=accum.device)
+    s = C.c_void_p(stream.cuda_stream) if stream is not None else C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _native.check(lib.ct_tonemap_device(C.c_void_p(accum.data_ptr()), width, height, float(samples),
+                                        float(exposure_ev), MODES[mode], C.c_void_p(out.data_ptr()), s))
+    return out
+
+
+def ppm_device(accum, width: int, height: int, samples: float, exposure_ev: float = 0.0, mode: str = "aces",
+               stream=None) -> bytes:
+    """tonemapBuffer + encodePPM on the GPU; returns the PPM file bytes."""
+    import ctypes as C
+
+    import torch
+
+    from . import _native
+
+    lib = _native.lib()
+    cap = 32 + width * height * 3
+    out = torch.empty(cap, dtype=torch.uint8, device=accum.device)
+    size = C.c_uint64()
+    s = C.c_void_p(stream.cuda_stream) if stream is not None else C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _native.check(lib.ct_ppm_device(C.c_void_p(accum.data_ptr()), width, height, float(samples), float(exposure_ev),
+                                    MODES[mode], C.c_void_p(out.data_ptr()), cap, C.byref(size), s))
+    return out[:size.value].cpu().numpy().tobytes()

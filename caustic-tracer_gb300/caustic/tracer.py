@@ -174,3 +174,37 @@ def render_image(scene: Union[Scene, PackedScene, DeviceScene], frame: CameraFra
     finally:
         if own is not None:
             own.close()
+
+
+@dataclass
+class PickResult:
+    """picking.ts:7-12."""
+
+    object_index: int
+    prim: int
+    t: float
+    point: tuple
+
+
+def pick_many(scene: DeviceScene, frame: CameraFrame, sx, sy):
+    """pick (picking.ts:21-33) for arrays of screen positions on the GPU (ct_pick):
+    returns (object, prim, t, point) arrays; object/prim -1 and t = inf on a miss."""
+    sx = np.ascontiguousarray(sx, np.float64).reshape(-1)
+    sy = np.ascontiguousarray(sy, np.float64).reshape(-1)
+    n = len(sx)
+    obj = np.empty(n, np.int32)
+    prim = np.empty(n, np.int32)
+    t = np.empty(n, np.float32)
+    point = np.empty((n, 3), np.float64)
+    f = frame.struct()
+    _native.check(scene._lib.ct_pick(scene.handle, C.byref(f), n, _native.ptr(sx), _native.ptr(sy), _native.ptr(obj),
+                                     _native.ptr(prim), _native.ptr(t), _native.ptr(point)))
+    return obj, prim, t, point
+
+
+def pick(scene: DeviceScene, frame: CameraFrame, sx: float, sy: float) -> Optional[PickResult]:
+    """pick (picking.ts:21-33): what the pinhole ray through (sx, sy) hits, or None."""
+    obj, prim, t, point = pick_many(scene, frame, [sx], [sy])
+    if prim[0] < 0:
+        return None
+    return PickResult(int(obj[0]), int(prim[0]), float(t[0]), tuple(float(v) for v in point[0]))

@@ -21,7 +21,7 @@ PKG = HERE.parent
 OUT_DIR = PKG / "_build"
 LIB = OUT_DIR / "libcaustic_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["pack_host.cpp", "profile.cpp", "scene.cu", "trace.cu", "integrator.cu", "batch.cu"]
+SOURCES = ["pack_host.cpp", "profile.cpp", "scene.cu", "trace.cu", "integrator.cu", "batch.cu", "display.cu"]
 HEADERS = ["common.hpp", "scene.hpp", "traverse.cuh", "integrator.cuh", "wavefront.cuh", "profile.hpp",
            "../../include/caustic.h"]
 

@@ -1,0 +1,143 @@
+// Display transforms on the device: tonemapBuffer (tonemap.ts:41-62) into
+// RGBA8 and a binary PPM (ppm.ts:4-16) straight from the sum buffer.
+//
+// Each channel is computed in float32 (ACES fit or Reinhard, then the sRGB
+// curve with powf); its scaled value y = 255 * srgb carries an error below
+// 3e-4. Only a channel whose y lies within 2e-3 of a rounding boundary
+// (k + 0.5), or is not a number, is recomputed in float64 in the reference's
+// operation order, so every byte is the one the reference's float64 code
+// stores. One thread per pixel: 12 bytes read, 4 (or 3) written.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+
+#include "scene.hpp"
+
+namespace ct {
+namespace {
+
+constexpr float kRoundMargin = 2e-3f;
+constexpr int kBlock = 256;
+
+// tonemap.ts:7-15 and 18-20, float64
+__device__ double aces64(double x) {
+  const double v = (x * (2.51 * x + 0.03)) / (x * (2.43 * x + 0.59) + 0.14);
+  return v < 0 ? 0 : v > 1 ? 1 : v;
+}
+__device__ double reinhard64(double x) { return x <= 0 ? 0 : x / (1 + x); }
+// tonemap.ts:27-31
+__device__ double srgb64(double x) {
+  if (x <= 0) return 0;
+  if (x >= 1) return 1;
+  return x <= 0.0031308 ? 12.92 * x : 1.055 * pow(x, 1 / 2.4) - 0.055;
+}
+// Math.round (halves toward +infinity), then the Uint8ClampedArray store
+// (clamp to [0, 255], NaN -> 0).
+__device__ uint8_t store_byte(double y) {
+  const double f = floor(y);
+  const double v = y - f >= 0.5 ? f + 1 : f;
+  return (uint8_t)(v >= 0 && v <= 255 ? v : v > 255 ? 255 : 0);
+}
+
+// The same curves in float32.
+__device__ float aces32(float x) {
+  const float v = (x * __fmaf_rn(2.51f, x, 0.03f)) / __fmaf_rn(x, __fmaf_rn(2.43f, x, 0.59f), 0.14f);
+  return v < 0.0f ? 0.0f : v > 1.0f ? 1.0f : v;
+}
+__device__ float reinhard32(float x) { return x <= 0.0f ? 0.0f : x / (1.0f + x); }
+__device__ float srgb32(float x) {
+  if (x <= 0.0f) return 0.0f;
+  if (x >= 1.0f) return 1.0f;
+  return x <= 0.0031308f ? 12.92f * x : __fmaf_rn(1.055f, powf(x, 1.0f / 2.4f), -0.055f);
+}
+
+__device__ __forceinline__ uint8_t channel(float a, double inv, float inv32, int aces) {
+  const float x = a * inv32;
+  const float y = srgb32(aces ? aces32(x) : reinhard32(x)) * 255.0f;
+  const float frac = y - floorf(y);
+  if (fabsf(frac - 0.5f) > kRoundMargin) return (uint8_t)(frac > 0.5f ? floorf(y) + 1.0f : floorf(y));
+  const double xd = (double)a * inv;  // near a boundary (or NaN): the reference's float64 path
+  return store_byte(srgb64(aces ? aces64(xd) : reinhard64(xd)) * 255.0);
+}
+
+// RGBA (stride 4, alpha 255) or the PPM payload (stride 3) after `offset`
+// header bytes, which block 0 writes from `header`.
+struct Header {
+  char bytes[32];
+  uint32_t len;
+};
+
+__global__ void __launch_bounds__(kBlock) k_tonemap(const float* __restrict__ accum, uint32_t pixels, double inv,
+                                                    float inv32, int aces, uint8_t* __restrict__ out,
+                                                    uint32_t stride, Header header) {
+  if (blockIdx.x == 0 && threadIdx.x < header.len) out[threadIdx.x] = (uint8_t)header.bytes[threadIdx.x];
+  uint8_t* px_out = out + header.len;
+  const uint32_t grid = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += grid) {
+    const float r = accum[3 * (size_t)i], g = accum[3 * (size_t)i + 1], b = accum[3 * (size_t)i + 2];
+    const uint8_t br = channel(r, inv, inv32, aces), bg = channel(g, inv, inv32, aces),
+                  bb = channel(b, inv, inv32, aces);
+    if (stride == 4) {
+      reinterpret_cast<uchar4*>(px_out)[i] = make_uchar4(br, bg, bb, 255);
+    } else {
+      uint8_t* o = px_out + 3 * (size_t)i;
+      o[0] = br, o[1] = bg, o[2] = bb;
+    }
+  }
+}
+
+ct_status launch_tonemap(const float* accum, int32_t width, int32_t height, double samples, double exposure_ev,
+                         int32_t mode, uint8_t* out, uint32_t stride, const Header& header, void* stream) {
+  const uint64_t pixels = (uint64_t)width * (uint64_t)height;
+  // tonemap.ts:49: inv = 2^ev / samples, 0 without samples
+  const double inv = samples > 0 ? std::pow(2.0, exposure_ev) / samples : 0.0;
+  int dev = 0, sms = 0;
+  CT_CUDA(cudaGetDevice(&dev));
+  CT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint64_t need = (pixels + kBlock - 1) / kBlock;
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sms * 8));
+  k_tonemap<<<grid, kBlock, 0, static_cast<cudaStream_t>(stream)>>>(accum, (uint32_t)pixels, inv, (float)inv,
+                                                                     mode == 0, out, stride, header);
+  CT_CUDA(cudaGetLastError());
+  return CT_OK;
+}
+
+ct_status check_image(const float* accum, int32_t width, int32_t height, int32_t mode, const void* out) {
+  CT_CHECK_ARG(accum != nullptr && out != nullptr, "NULL device pointer");
+  CT_CHECK_ARG(width > 0 && height > 0, "image size %dx%d is not positive", width, height);
+  CT_CHECK_ARG((uint64_t)width * (uint64_t)height <= (1ull << 30), "image of %dx%d pixels is too large", width, height);
+  CT_CHECK_ARG(mode == 0 || mode == 1, "tone map mode %d is not 0 (ACES) or 1 (Reinhard)", mode);
+  return CT_OK;
+}
+
+}  // namespace
+}  // namespace ct
+
+extern "C" {
+
+ct_status ct_tonemap_device(const float* accum, int32_t width, int32_t height, double samples, double exposure_ev,
+                            int32_t mode, uint8_t* rgba, void* stream) {
+  ct::clear_error();
+  ct_status st = ct::check_image(accum, width, height, mode, rgba);
+  if (st != CT_OK) return st;
+  CT_CHECK_ARG(((uintptr_t)rgba & 3u) == 0, "rgba must be 4-byte aligned");
+  return ct::launch_tonemap(accum, width, height, samples, exposure_ev, mode, rgba, 4, ct::Header{{0}, 0}, stream);
+}
+
+ct_status ct_ppm_device(const float* accum, int32_t width, int32_t height, double samples, double exposure_ev,
+                        int32_t mode, uint8_t* ppm, uint64_t capacity, uint64_t* size, void* stream) {
+  ct::clear_error();
+  ct_status st = ct::check_image(accum, width, height, mode, ppm);
+  if (st != CT_OK) return st;
+  ct::Header h{};
+  const int n = std::snprintf(h.bytes, sizeof h.bytes, "P6\n%d %d\n255\n", width, height);
+  CT_CHECK_ARG(n > 0 && n < (int)sizeof h.bytes, "PPM header does not fit");
+  h.len = (uint32_t)n;
+  const uint64_t total = h.len + (uint64_t)width * (uint64_t)height * 3;
+  if (size) *size = total;
+  CT_CHECK_ARG(capacity >= total, "PPM needs %llu bytes, buffer holds %llu", (unsigned long long)total,
+               (unsigned long long)capacity);
+  return ct::launch_tonemap(accum, width, height, samples, exposure_ev, mode, ppm, 3, h, stream);
+}
+
+}  // extern "C"

@@ -7,7 +7,10 @@
 // loads (32 B). Closest hits whose float32 distance bound is loose are
 // flagged and recomputed in float64 by a separate, converged pass.
 #include <atomic>
+#include <cmath>
 #include <cstring>
+#include <new>
+#include <vector>
 
 #include "profile.hpp"
 #include "scene.hpp"
@@ -207,10 +210,93 @@ ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, 
   return CT_OK;
 }
 
+// Object index of each hit primitive (-1 on a miss).
+__global__ void k_pick_objects(const uint32_t* __restrict__ prim_object, const int32_t* __restrict__ prim,
+                               uint32_t n, int32_t* __restrict__ object) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) object[i] = prim[i] >= 0 ? (int32_t)prim_object[prim[i]] : -1;
+}
+
+// camera.ts:62-77 primaryRay (generateRay with a zero lens sample), float64
+// in the reference's operation order.
+void primary_ray(const ct_camera_frame& f, double sx, double sy, double o[3], double d[3]) {
+  const double px = (2 * sx - 1) * f.tan_half_fov * f.aspect;
+  const double py = (2 * sy - 1) * f.tan_half_fov;
+  double focus[3], dir[3];
+  for (int k = 0; k < 3; k++)
+    focus[k] = f.origin[k] + ((f.right[k] * px + f.up[k] * py) + f.forward[k]) * f.focus_distance;
+  for (int k = 0; k < 3; k++) {
+    const double offset = f.right[k] * (0 * f.lens_radius) + f.up[k] * (0 * f.lens_radius);
+    o[k] = f.origin[k] + offset;
+    dir[k] = focus[k] - o[k];
+  }
+  const double len = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);  // vec3.ts:26-31
+  for (int k = 0; k < 3; k++) d[k] = len > 0 ? dir[k] * (1 / len) : 0.0;
+}
+
+ct_status pick(ct_scene* s, const ct_camera_frame* frame, uint32_t n, const double* sx, const double* sy,
+               int32_t* object, int32_t* prim, float* t, double* point) {
+  CT_CHECK_ARG(s != nullptr && frame != nullptr, "NULL scene or frame");
+  CT_CHECK_ARG(n == 0 || (sx && sy && object && prim && t), "NULL host pointer");
+  if (n == 0) return CT_OK;
+  std::vector<float> rays((size_t)n * CT_RAY_FLOATS);
+  std::vector<double> ray64((size_t)n * 6);
+  for (uint32_t i = 0; i < n; i++) {
+    double* o = &ray64[(size_t)i * 6];
+    primary_ray(*frame, sx[i], sy[i], o, o + 3);
+    float* r = &rays[(size_t)i * CT_RAY_FLOATS];
+    for (int k = 0; k < 6; k++) r[k] = (float)o[k];
+    r[6] = (float)1e-4;  // T_MIN (intersect.ts:14)
+    r[7] = INFINITY;
+  }
+  std::lock_guard<std::mutex> guard(s->lock);
+  CT_CUDA(cudaSetDevice(s->device));
+  const size_t ray_bytes = rays.size() * sizeof(float);
+  ct_status st = s->io.reserve(ray_bytes + (size_t)n * 12, &s->device_bytes);
+  if (st != CT_OK) return st;
+  char* base = s->io.as<char>();
+  float* d_rays = reinterpret_cast<float*>(base);
+  int32_t* d_prim = reinterpret_cast<int32_t*>(base + ray_bytes);
+  float* d_t = reinterpret_cast<float*>(d_prim + n);
+  int32_t* d_obj = reinterpret_cast<int32_t*>(d_t + n);
+  cudaStream_t stream = s->stream;
+  CT_CUDA(cudaMemsetAsync(s->counters.ptr, 0, 2 * sizeof(uint32_t), stream));
+  CT_CUDA(cudaMemcpyAsync(d_rays, rays.data(), ray_bytes, cudaMemcpyHostToDevice, stream));
+  st = launch<false>(s, d_rays, n, d_prim, d_t, nullptr, nullptr, nullptr, stream);
+  if (st != CT_OK) return st;
+  k_pick_objects<<<(n + 255) / 256, 256, 0, stream>>>(s->prim_object.as<uint32_t>(), d_prim, n, d_obj);
+  CT_CUDA(cudaGetLastError());
+  CT_CUDA(cudaMemcpyAsync(prim, d_prim, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+  CT_CUDA(cudaMemcpyAsync(t, d_t, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+  CT_CUDA(cudaMemcpyAsync(object, d_obj, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+  uint32_t counters[2] = {0, 0};
+  CT_CUDA(cudaMemcpyAsync(counters, s->counters.ptr, sizeof counters, cudaMemcpyDeviceToHost, stream));
+  CT_CUDA(cudaStreamSynchronize(stream));
+  if (counters[1]) return fail(CT_ERR_UNSUPPORTED, "traversal stack overflow (stack need %u)", s->stack_need);
+  if (point) {
+    for (uint32_t i = 0; i < n; i++) {  // picking.ts:32: origin + dir * t
+      const double* o = &ray64[(size_t)i * 6];
+      for (int k = 0; k < 3; k++)
+        point[(size_t)i * 3 + k] = prim[i] >= 0 ? o[k] + o[3 + k] * (double)t[i] : NAN;
+    }
+  }
+  return CT_OK;
+}
+
 }  // namespace
 }  // namespace ct
 
 extern "C" {
+
+ct_status ct_pick(ct_scene* scene, const ct_camera_frame* frame, uint32_t count, const double* sx, const double* sy,
+                  int32_t* object, int32_t* prim, float* t, double* point) {
+  ct::clear_error();
+  try {
+    return ct::pick(scene, frame, count, sx, sy, object, prim, t, point);
+  } catch (const std::bad_alloc&) {
+    return ct::fail(CT_ERR_OUT_OF_MEMORY, "ct_pick: host allocation failed");
+  }
+}
 
 int32_t ct_set_traversal(int32_t variant) {
   return ct::g_variant.exchange(variant == 1 ? 1 : 0);

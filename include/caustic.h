@@ -315,6 +315,31 @@ ct_status ct_accumulate_pass_noalloc(ct_scene* scene, const ct_camera_frame* fra
                                      int32_t height, uint32_t frame_index, const ct_trace_options* opts,
                                      float* accum, void* stream);
 
+/* ---- either side of the path ----------------------------------------------
+ * tonemapBuffer (tonemap.ts:41-62) on the device: the sum buffer `accum`
+ * (width*height*3 floats, device) divided by `samples`, scaled by
+ * 2^exposure_ev, tone mapped (mode 0 = ACES fit, 1 = Reinhard), sRGB encoded
+ * and rounded like Math.round into `rgba` (width*height*4 bytes, device,
+ * 4-byte aligned, alpha 255). Every byte equals the reference's float64
+ * result (float32 with a float64 recomputation near rounding boundaries).
+ * Enqueued on `stream` (cudaStream_t, NULL = default stream).              */
+ct_status ct_tonemap_device(const float* accum, int32_t width, int32_t height, double samples,
+                            double exposure_ev, int32_t mode, uint8_t* rgba, void* stream);
+/* tonemapBuffer then encodePPM (ppm.ts:4-16) on the device: writes the
+ * binary PPM file (header "P6\n<w> <h>\n255\n", then RGB rows from the top)
+ * into `ppm` (device, `capacity` bytes); *size receives the file size. A
+ * buffer that is too small is rejected (CT_ERR_INVALID_ARGUMENT, *size set). */
+ct_status ct_ppm_device(const float* accum, int32_t width, int32_t height, double samples, double exposure_ev,
+                        int32_t mode, uint8_t* ppm, uint64_t capacity, uint64_t* size, void* stream);
+/* pick (picking.ts:21-33) for `count` screen positions (sx, sy in [0, 1],
+ * sy = 1 at the top): the pinhole ray of primaryRay (camera.ts:75) in
+ * float64, rounded to the float32 ray record, tMin = T_MIN; closest hit as
+ * ct_trace_closest. object[i] = primObject[prim] or -1, prim[i], t[i]
+ * (+inf on a miss), point[3i..3i+2] = origin + dir * t in float64 (NaN on a
+ * miss; `point` may be NULL). Host pointers.                               */
+ct_status ct_pick(ct_scene* scene, const ct_camera_frame* frame, uint32_t count, const double* sx,
+                  const double* sy, int32_t* object, int32_t* prim, float* t, double* point);
+
 /* ---- profiling ------------------------------------------------------------
  * No counterpart in the reference (which times with performance.now(),
  * reference.ts:28,42). While enabled, every kernel launch is bracketed by

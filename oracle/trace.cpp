@@ -898,7 +898,8 @@ void tonemap_buffer(const float* accum, int width, int height, double samples, d
       double x = accum[(size_t)i * 3 + k] * inv;
       double mapped = aces ? aces_fitted(x) : reinhard(x);
       double v = js_round(linear_to_srgb(mapped) * 255);
-      rgba[(size_t)i * 4 + k] = (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v);
+      // Uint8ClampedArray store: clamp to [0, 255], NaN -> 0
+      rgba[(size_t)i * 4 + k] = (uint8_t)(v >= 0 && v <= 255 ? v : v > 255 ? 255 : 0);
     }
     rgba[(size_t)i * 4 + 3] = 255;
   }
