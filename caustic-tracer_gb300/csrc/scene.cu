@@ -374,6 +374,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   d.mats = s->mats.as<float4>();
   d.lights = s->lights.as<int32_t>();
   d.prim_object = s->prim_object.as<uint32_t>();
+  d.prim_count = v.prim_count;
   d.node_count = v.node_count;
   d.light_count = v.light_count;
   if (v.node_count > 0) {

@@ -40,6 +40,7 @@ struct SceneDev {
   const float4* __restrict__ mats;   // 4 per material (pack.ts:12-16)
   const int32_t* __restrict__ lights;
   const uint32_t* __restrict__ prim_object;
+  uint32_t prim_count;
   uint32_t node_count;
   uint32_t light_count;
   int32_t root_ref;
@@ -587,6 +588,19 @@ __device__ __forceinline__ bool walk_ordered(const SceneDev& s, const RayF& r, H
   while (w.ref != kWalkDone) walk_step<EXACT>(s, w, fallbacks);
   h = w.h;
   return !w.overflow;
+}
+
+// Scenes of at most kBrutePrims primitives: every primitive tested in packed
+// order, no boxes. The skip-link walk visits leaves in node-array order, and
+// the leaves of that order cover the primitives contiguously in packed order,
+// so this is the same sequence of primitive tests minus those the walk's
+// (conservative) box tests would skip; every lane runs the same instructions.
+constexpr uint32_t kBrutePrims = 32;
+
+template <bool EXACT>
+__device__ __forceinline__ void walk_all(const SceneDev& s, const RayF& r, HitF& h, bool any, uint32_t& fallbacks) {
+  for (uint32_t p = 0; p < s.prim_count; p++)
+    if (test_prim<EXACT>(s, r, p, h, any, fallbacks)) return;
 }
 
 // Stackless skip-link walk over the reference node array, the literal

@@ -194,7 +194,9 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
 //   kWalkPersistent ordered walk, lanes refill from a work counter as their
 //                   walks finish (pays off for deep trees);
 //   kWalkSkip       the reference's stackless skip-link walk (no stack; all
-//                   lanes visit nodes in the same order; for small trees);
+//                   lanes visit nodes in the same order; for small trees;
+//                   scenes of <= 32 primitives test every primitive in the
+//                   order the walk would, without boxes);
 //   kWalkPerJob     BATCH only, a planning mode: each job walks as its scene
 //                   does alone; a wave holds jobs of one walk and runs its
 //                   kernel.
@@ -272,7 +274,10 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
       const ctk::SceneDev sc = BATCH ? job_of(i).scene : a.scene;
       if constexpr (FORM == kWalkSkip) {
         w.h = ctk::HitF{-1, w.r.tmax, 0.0f, 0.0f, 0.0f};
-        ctk::walk_stackless<false>(sc, w.r, w.h, i >= n_ext, fallbacks);
+        if (sc.prim_count <= ctk::kBrutePrims)
+          ctk::walk_all<false>(sc, w.r, w.h, i >= n_ext, fallbacks);
+        else
+          ctk::walk_stackless<false>(sc, w.r, w.h, i >= n_ext, fallbacks);
       } else {
         ctk::walk_begin(sc, w, i >= n_ext);
         while (w.ref != ctk::kWalkDone) ctk::walk_step<false>(sc, w, fallbacks);

@@ -104,3 +104,24 @@ def test_degenerate_inputs(oracle, packed):  # bvh.test.ts:148-169
     assert rep["ok"] and rep["max_leaf"] <= 4
     p, t, *_ = oracle.trace(co, np.array([[1, 2, -5, 0, 0, 1, 1e-4, np.inf]], np.float32), 0)
     assert p[0] >= 0 and abs(t[0] - 7.5) < 1e-5
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_leaves_in_node_order_cover_primitives_in_packed_order(seed):
+    """The stackless walk visits leaves in node-array order; they must cover
+    the primitives contiguously in packed order (the GPU's small-scene form
+    tests primitives in that order and relies on it)."""
+    import caustic as ct
+
+    scenes = [ct.CORNELL_BOX, ct.cornell_unit_box(), ct.random_test_scene(ct.Rng(seed), 10 * seed, 20 * seed),
+              ct.batch_scene(seed, 40 * seed, 3 * seed)]
+    for sc in scenes:
+        p = ct.pack_scene(sc)
+        nodes = np.asarray(p.nodes).reshape(-1, 8)
+        nxt = 0
+        for row in nodes:
+            if row[7] >= 0:
+                word = int(row[7])
+                assert word >> 3 == nxt, sc.name
+                nxt += word & 7
+        assert nxt == p.prim_count, sc.name
