@@ -104,27 +104,38 @@ struct WaveArgs {
 // counters.
 inline size_t wave_counter_words(int32_t max_bounces) { return 3 * (size_t)max_bounces + 12; }
 
-// Block-wide stream compaction: returns the output slot of this thread (valid
-// when pred) and appends the block's survivors contiguously with one atomic.
-__device__ __forceinline__ uint32_t block_append(bool pred, uint32_t* counter, uint32_t* s_warp, uint32_t* s_base) {
+// Block-wide stream compaction of two predicates at once: warp ballots, an
+// intra-block prefix sum over the warp counts and one atomicAdd per counter
+// per block, so the block's survivors of each predicate land contiguously.
+// Returns slot_a in *counter_a (valid when pa) and slot_b in *counter_b
+// (valid when pb). s_warp holds 2*kWarps words, s_base two.
+__device__ __forceinline__ void block_append2(bool pa, bool pb, uint32_t* counter_a, uint32_t* counter_b,
+                                              uint32_t* s_warp, uint32_t* s_base, uint32_t& slot_a,
+                                              uint32_t& slot_b) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t mask = __ballot_sync(0xffffffffu, pred);
-  const uint32_t rank = __popc(mask & ((1u << lane) - 1u));
-  if (lane == 0) s_warp[warp] = __popc(mask);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t total = 0;
-    for (int w = 0; w < kWarps; w++) {
-      const uint32_t c = s_warp[w];
-      s_warp[w] = total;
-      total += c;
-    }
-    *s_base = total ? atomicAdd(counter, total) : 0u;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t ma = __ballot_sync(0xffffffffu, pa), mb = __ballot_sync(0xffffffffu, pb);
+  if (lane == 0) {
+    s_warp[warp] = __popc(ma);
+    s_warp[kWarps + warp] = __popc(mb);
   }
   __syncthreads();
-  const uint32_t slot = *s_base + s_warp[warp] + rank;
+  if (threadIdx.x == 0) {
+    uint32_t ta = 0, tb = 0;
+    for (int w = 0; w < kWarps; w++) {
+      const uint32_t ca = s_warp[w], cb = s_warp[kWarps + w];
+      s_warp[w] = ta;
+      s_warp[kWarps + w] = tb;
+      ta += ca;
+      tb += cb;
+    }
+    s_base[0] = ta ? atomicAdd(counter_a, ta) : 0u;
+    s_base[1] = tb ? atomicAdd(counter_b, tb) : 0u;
+  }
   __syncthreads();
-  return slot;
+  slot_a = s_base[0] + s_warp[warp] + __popc(ma & lt);
+  slot_b = s_base[1] + s_warp[kWarps + warp] + __popc(mb & lt);
+  __syncthreads();
 }
 
 // Chunk holding path p (KEY = path0) or accumulation item p (KEY = acc0);
@@ -288,9 +299,11 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
   if (fallbacks) atomicAdd(a.counts + 2 * a.max_bounces + 6, fallbacks);
 }
 
+// 10 blocks of 128 per SM (48 registers, ~50 bytes spilled): 3 % faster on
+// the Cornell box than 8 blocks at 64 registers.
 template <bool BATCH>
-__global__ void __launch_bounds__(kBlock) k_shade(WaveArgs a, int32_t bounce) {
-  __shared__ uint32_t s_warp[kWarps], s_base;
+__global__ void __launch_bounds__(kBlock, 10) k_shade(WaveArgs a, int32_t bounce) {
+  __shared__ uint32_t s_warp[2 * kWarps], s_base[2];
   const uint32_t n = a.counts[bounce];
   uint32_t* next_count = a.counts + bounce + 1;
   uint32_t* shadow_count = a.counts + a.max_bounces + 2 + bounce;
@@ -414,8 +427,8 @@ __global__ void __launch_bounds__(kBlock) k_shade(WaveArgs a, int32_t bounce) {
         *L = l;
       }
     }
-    const uint32_t slot = block_append(cont, next_count, s_warp, &s_base);
-    const uint32_t sslot = block_append(shadow, shadow_count, s_warp, &s_base);
+    uint32_t slot, sslot;
+    block_append2(cont, shadow, next_count, shadow_count, s_warp, s_base, slot, sslot);
     if (cont) {
       a.next.a[slot] = na;
       a.next.b[slot] = nb;
