@@ -64,6 +64,8 @@ def parse_args():
     ap.add_argument("--rays", type=int, default=0, help="traversal: trace only this many rays (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0,
+                    help="--impl reference: seconds of oracle work in the calibration run (a step is a quarter)")
     return ap.parse_args()
 
 
@@ -281,17 +283,18 @@ def kernel_bytes_per_step(kernel: str, cpu: dict, units_per_step: int):
 
 def run_reference(args, rank, world):
     """The reference algorithm on the host cores: W warm-up and K timed steps, each step
-    one bounded sample of the workload (sized by a calibration run to ~2 s)."""
+    one bounded sample of the workload (sized by a calibration run to cpu_seconds / 4, 2 s by default)."""
     if rank != 0:
         return
     import oracle_lib as oracle
     from caustic import _abi
 
     threads = os.cpu_count() or 1
-    rec = cpu_reference(args.workload, args.small, target_s=8.0)
+    rec = cpu_reference(args.workload, args.small, target_s=args.cpu_seconds)
+    step_s = args.cpu_seconds / 4
     if args.workload == "traversal":
         packed, rays = traversal_inputs(0, args.small)
-        n = max(1 << 12, min(len(rays), int(rec["value"] * 1e6 * 2.0)))
+        n = max(1 << 12, min(len(rays), int(rec["value"] * 1e6 * step_s)))
         sample = rays[:n]
         units = n
 
@@ -302,7 +305,7 @@ def run_reference(args, rank, world):
     else:
         packed, frame, cfg = render_inputs(args.workload, args.small)
         w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
-        rows = max(1, min(h, int(rec["value"] * 1e6 * 2.0 / (w * spp))))
+        rows = max(1, min(h, int(rec["value"] * 1e6 * step_s / (w * spp))))
         opts = _abi.ct_render_options(w, rows, spp, cfg["max_bounces"], int(cfg["russian_roulette"]),
                                       int(cfg["nee"]), cfg["seed"])
         fs = frame.struct()
