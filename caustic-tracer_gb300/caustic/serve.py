@@ -53,9 +53,11 @@ class Request:
 @dataclass
 class Result:
     request: Request
-    image: Optional[np.ndarray]
-    admitted: float
+    image: Optional[np.ndarray]  # None unless status == "done"
+    admitted: Optional[float]    # None for a request cancelled before admission
     finished: float
+    status: str = "done"         # "done", "cancelled" or "failed"
+    error: Optional[str] = None
 
     @property
     def latency(self) -> float:
@@ -70,6 +72,9 @@ class _Active:
     done: int = 0    # passes completed
     admitted: float = 0.0
     buffer: object = None
+    inflight: int = 0                # steps in flight that hold passes of this request
+    stop: Optional[str] = None       # "cancelled" or "failed": leaves once nothing is in flight
+    error: Optional[str] = None
 
 
 class Executor(Protocol):
@@ -116,6 +121,43 @@ class RenderServer:
     def submit(self, req: Request) -> None:
         self.waiting.append(req)
 
+    def cancel(self, rid: int) -> bool:
+        """Cancels request `rid`: a waiting request leaves at once; an admitted
+        one takes no further passes and leaves (its buffer released) when the
+        steps in flight that hold its passes have completed. Returns whether
+        the request was found."""
+        for req in list(self.waiting):
+            if req.rid == rid:
+                self.waiting.remove(req)
+                self.results.append(Result(req, None, None, self.clock(), "cancelled"))
+                return True
+        for a in self.active:
+            if a.req.rid == rid and a.stop is None:
+                a.stop = "cancelled"
+                if a.inflight == 0:
+                    self._retire(a)
+                return True
+        return False
+
+    def _retire(self, a: _Active, image=None) -> None:
+        status = a.stop or "done"
+        self.results.append(Result(a.req, image if status == "done" else None, a.admitted, self.clock(), status,
+                                   a.error))
+        self.ex.release(a.buffer)
+        self.active.remove(a)
+        n = self.scenes_in_use[a.req.scene] - 1
+        if n:
+            self.scenes_in_use[a.req.scene] = n
+        else:
+            del self.scenes_in_use[a.req.scene]
+
+    def _fail(self, plan, err: Exception) -> None:
+        for a, _ in plan:
+            if a.stop is None:
+                a.stop, a.error = "failed", f"{type(err).__name__}: {err}"
+            if a.inflight == 0 and a in self.active:
+                self._retire(a)
+
     def _admit(self) -> None:
         while self.waiting:
             req = self.waiting[0]
@@ -139,7 +181,7 @@ class RenderServer:
         hot in L2 for a while) and at least one pass, at most what it still
         needs and what still fits; requests that do not fit wait for the next
         step, which starts at the first of them."""
-        pending = [a for a in self.active if a.issued < a.req.spp]
+        pending = [a for a in self.active if a.issued < a.req.spp and a.stop is None]
         if not pending:
             return []
         pending.sort(key=lambda a: a.seq)
@@ -173,21 +215,24 @@ class RenderServer:
 
     def _complete_oldest(self) -> int:
         ticket, plan = self.inflight.popleft()
-        self.ex.wait(ticket)
+        for a, _ in plan:
+            a.inflight -= 1
+        try:
+            self.ex.wait(ticket)
+        except Exception as err:  # the step failed on the device: its requests fail, the server goes on
+            self._fail(plan, err)
+            return 0
         rendered = 0
         for a, p in plan:
+            if a not in self.active:
+                continue
             a.done += p
             rendered += p * a.req.pixels
-            if a.done >= a.req.spp:
-                img = self.ex.fetch(a.req, a.buffer)
-                self.results.append(Result(a.req, img, a.admitted, self.clock()))
-                self.ex.release(a.buffer)
-                self.active.remove(a)
-                n = self.scenes_in_use[a.req.scene] - 1
-                if n:
-                    self.scenes_in_use[a.req.scene] = n
-                else:
-                    del self.scenes_in_use[a.req.scene]
+            if a.stop is not None:
+                if a.inflight == 0:
+                    self._retire(a)
+            elif a.done >= a.req.spp:
+                self._retire(a, self.ex.fetch(a.req, a.buffer))
         self.samples += rendered
         return rendered
 
@@ -198,14 +243,23 @@ class RenderServer:
         self._admit()
         plan = self._plan()
         if plan:
-            ticket = self.ex.launch([(a.req, a.buffer, a.issued, p) for a, p in plan])
-            for a, p in plan:
-                a.issued += p
-            self.inflight.append((ticket, plan))
-            self.steps += 1
+            try:
+                ticket = self.ex.launch([(a.req, a.buffer, a.issued, p) for a, p in plan])
+            except Exception as err:  # e.g. a failed upload or launch: these requests fail
+                self._fail(plan, err)
+                plan = []
+            else:
+                for a, p in plan:
+                    a.issued += p
+                    a.inflight += 1
+                self.inflight.append((ticket, plan))
+                self.steps += 1
         if self.inflight and (len(self.inflight) >= STEPS_IN_FLIGHT or not plan):
             return self._complete_oldest()
         return 0
+
+    def __len__(self) -> int:
+        return len(self.waiting) + len(self.active)
 
     def busy(self) -> bool:
         return bool(self.waiting or self.active or self.inflight)
@@ -235,7 +289,8 @@ class RenderServer:
 
 
 def latency_stats(results: Sequence[Result]) -> dict:
-    lat = np.array([r.latency for r in results], dtype=np.float64) * 1e3
+    """Latency percentiles (ms) of the completed requests."""
+    lat = np.array([r.latency for r in results if r.status == "done"], dtype=np.float64) * 1e3
     if len(lat) == 0:
         return {"p50_ms": None, "p99_ms": None, "mean_ms": None}
     return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),

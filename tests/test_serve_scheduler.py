@@ -1,5 +1,7 @@
 """Serving scheduler (host logic) with a fake executor: admission by memory
 budget, progressive chunks, retirement, and the waiting queue."""
+import pytest
+
 import caustic as ct
 from caustic.serve import PATH_STATE_BYTES, STEPS_IN_FLIGHT, RenderServer, Request
 
@@ -154,3 +156,60 @@ def test_steps_fill_one_wave_and_never_mix_walk_classes():
     assert sorted(r.request.rid for r in srv.results) == sorted(list(range(len(sides))) + [99])
     for res in srv.results:
         assert sum(p for _, p in res.image) == res.request.spp
+
+
+class FailingExecutor(FakeExecutor):
+    """Fails the launch of step `bad_launch` and the completion of step `bad_wait` (1-based)."""
+
+    def __init__(self, sb, bad_launch=None, bad_wait=None):
+        super().__init__(sb)
+        self.bad_launch, self.bad_wait, self.launches = bad_launch, bad_wait, 0
+
+    def launch(self, items):
+        self.launches += 1
+        if self.launches == self.bad_launch:
+            raise RuntimeError("simulated upload failure")
+        return super().launch(items)
+
+    def wait(self, ticket):
+        super().wait(ticket)
+        if ticket == self.bad_wait:
+            raise RuntimeError("simulated device error")
+
+
+@pytest.mark.parametrize("bad_launch,bad_wait", [(2, None), (None, 2), (1, 3)])
+def test_a_failed_step_fails_its_requests_and_the_server_goes_on(bad_launch, bad_wait):
+    ex = FailingExecutor({"a": 0}, bad_launch, bad_wait)
+    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=64 * 64 * 2, min_chunk_paths=0, clock=Clock())
+    for i in range(8):
+        srv.submit(_req(i, 64, 5))
+    srv.drain()
+    assert sorted(r.request.rid for r in srv.results) == list(range(8))  # every request answered once
+    failed = [r for r in srv.results if r.status == "failed"]
+    done = [r for r in srv.results if r.status == "done"]
+    assert failed and done
+    assert all("simulated" in r.error and r.image is None for r in failed)
+    for r in done:  # the others got every pass, in order
+        assert sum(p for _, p in r.image) == r.request.spp
+    assert not ex.live and not srv.active and not srv.inflight  # every buffer released
+
+
+def test_cancel_waiting_and_in_flight_requests():
+    ex = FakeExecutor({"a": 0})
+    step_paths = 64 * 64 * 2
+    budget = STEPS_IN_FLIGHT * step_paths * PATH_STATE_BYTES + 2 * 64 * 64 * 12  # two requests at a time
+    srv = RenderServer(ex, budget_bytes=budget, step_paths=step_paths, min_chunk_paths=0, clock=Clock())
+    for i in range(4):
+        srv.submit(_req(i, 64, 9))
+    srv.step()
+    assert {a.req.rid for a in srv.active} == {0, 1}
+    assert srv.cancel(3)  # still waiting
+    assert srv.cancel(0)  # admitted, passes in flight
+    assert not srv.cancel(42)
+    srv.drain()
+    status = {r.request.rid: r.status for r in srv.results}
+    assert status == {0: "cancelled", 1: "done", 2: "done", 3: "cancelled"}
+    issued0 = sum(p for items in ex.steps for rid, _, p in items if rid == 0)
+    assert issued0 < 9  # no passes launched after the cancel
+    assert not any(rid == 3 for items in ex.steps for rid, _, _ in items)
+    assert not ex.live
