@@ -295,6 +295,9 @@ constexpr float kReportRel = 1e-6f;
 __device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
 
+// Division-free until a hit is certain: u, v and t are compared as
+// numerators against |det| (one reciprocal per accepted candidate instead of
+// one per test).
 __device__ __forceinline__ bool tri_fast(const RayF& r, float4 a4, float4 b4, float4 c4, float closest, Cand& c) {
   const float e1x = b4.x - a4.x, e1y = b4.y - a4.y, e1z = b4.z - a4.z;
   const float e2x = c4.x - a4.x, e2y = c4.y - a4.y, e2z = c4.z - a4.z;
@@ -303,21 +306,24 @@ __device__ __forceinline__ bool tri_fast(const RayF& r, float4 a4, float4 b4, fl
   const float pz = fm(r.dx, e2y, -mul(r.dy, e2x));
   const float det = fm(e1x, px, fm(e1y, py, mul(e1z, pz)));
   if (det > -1e-12f && det < 1e-12f) return false;
-  const float inv = 1.0f / det;
+  const float ad = fabsf(det), sg = det < 0.0f ? -1.0f : 1.0f;
   const float tx = r.ox - a4.x, ty = r.oy - a4.y, tz = r.oz - a4.z;
-  const float u = mul(fm(tx, px, fm(ty, py, mul(tz, pz))), inv);
-  if (u < 0.0f || u > 1.0f) return false;
+  const float su = sg * fm(tx, px, fm(ty, py, mul(tz, pz)));  // u * |det|
+  if (su < 0.0f || su > ad) return false;
   const float qx = fm(ty, e1z, -mul(tz, e1y));
   const float qy = fm(tz, e1x, -mul(tx, e1z));
   const float qz = fm(tx, e1y, -mul(ty, e1x));
-  const float v = mul(fm(r.dx, qx, fm(r.dy, qy, mul(r.dz, qz))), inv);
-  if (v < 0.0f || u + v > 1.0f) return false;
-  const float t = mul(fm(e2x, qx, fm(e2y, qy, mul(e2z, qz))), inv);
+  const float sv = sg * fm(r.dx, qx, fm(r.dy, qy, mul(r.dz, qz)));  // v * |det|
+  if (sv < 0.0f || su + sv > ad) return false;
+  const float st = sg * fm(e2x, qx, fm(e2y, qy, mul(e2z, qz)));  // t * |det|
+  if (st <= r.tmin * ad || st >= closest * ad) return false;
+  const float inv = 1.0f / ad;
+  const float t = st * inv;
   if (t <= r.tmin || t >= closest) return false;
   c.t = t;
   c.e = 0.0f;
-  c.u = u;
-  c.v = v;
+  c.u = su * inv;
+  c.v = sv * inv;
   return true;
 }
 
@@ -329,9 +335,10 @@ __device__ __forceinline__ bool sphere_fast(const RayF& r, float4 c4, float rad,
   const float disc = fm(hb, hb, -mul(a, cc));
   if (disc < 0.0f) return false;
   const float s = sqrtf(disc);
-  float t = (-hb - s) / a;
+  const float inva = 1.0f / a;
+  float t = (-hb - s) * inva;
   if (t <= r.tmin || t >= closest) {
-    t = (-hb + s) / a;
+    t = (-hb + s) * inva;
     if (t <= r.tmin || t >= closest) return false;
   }
   c.t = t;
