@@ -60,6 +60,9 @@ def parse_args():
     ap.add_argument("--workload", choices=["cornell", "traversal", "caustic", "batched", "served"], default="cornell")
     ap.add_argument("--jobs", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--requests", type=int, default=128, help="served: number of requests")
+    ap.add_argument("--trace", choices=["c5", "preview"], default="c5",
+                    help="served: the request mix (c5: 128-1024 squared, 1-256 spp; preview: 128-256 squared, "
+                         "1-8 spp)")
     ap.add_argument("--small", action="store_true", help="reduced sizes for profiling captures")
     ap.add_argument("--rays", type=int, default=0, help="traversal: trace only this many rays (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -677,7 +680,7 @@ def run_batched(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
-def served_inputs(count: int, small: bool, rank: int):
+def served_inputs(count: int, small: bool, rank: int, trace: str = "c5"):
     """Scene pool and request trace of the served workload. Pool: the 256
     batched-workload soups, the unit Cornell box and the caustic scene.
     Requests: `count`, each drawing a scene from the pool, a square side in
@@ -694,9 +697,11 @@ def served_inputs(count: int, small: bool, rank: int):
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         packed = dict(zip(pool, ex.map(ct.pack_scene, pool.values())))
     frames = {k: (lambda a, cam=s.camera: ct.camera_frame(cam, a)) for k, s in pool.items()}
-    sides = (128, 256, 384) if small else tuple(range(128, 1025, 128))
-    reqs = poisson_requests(list(pool), frames, count, rate=1.0, seed=4242 + rank, sides=sides,
-                            max_spp=64 if small else 256)
+    if trace == "preview":  # interactive previews: small images, few passes
+        sides, max_spp = (128, 192, 256), 8
+    else:
+        sides, max_spp = ((128, 256, 384), 64) if small else (tuple(range(128, 1025, 128)), 256)
+    reqs = poisson_requests(list(pool), frames, count, rate=1.0, seed=4242 + rank, sides=sides, max_spp=max_spp)
     return packed, reqs
 
 
@@ -715,7 +720,7 @@ def run_served(args, rank, world):
     device = torch.device("cuda", torch.cuda.current_device())
     opts = ct.TraceOptions(max_bounces=8, russian_roulette=True, nee=True)
     count = 32 if args.small else args.requests
-    packed, trace = served_inputs(count, args.small, rank)
+    packed, trace = served_inputs(count, args.small, rank, args.trace)
     dev = {k: ct.DeviceScene(p) for k, p in packed.items()}
     samples = sum(r.pixels * r.spp for r in trace)
 
@@ -726,9 +731,9 @@ def run_served(args, rank, world):
             r.arrival = 0.0 if rate is None else r.arrival / rate
         return out
 
-    def served(rate=None):
+    def served(rate=None, policy="round_robin"):
         ex = GpuExecutor(dev, opts)
-        srv = RenderServer(ex)
+        srv = RenderServer(ex, policy=policy)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         e0.record(ex.stream)
@@ -763,16 +768,20 @@ def run_served(args, rank, world):
     # latency under Poisson arrivals at 80% of the plain path's request capacity
     rate = 0.8 * len(trace) / t_plain
     res_s, _, _, srv_s = served(rate)
+    res_f, _, _, _ = served(rate, "fifo")
     res_p, _ = plain(rate)
+    if args.trace == "preview":
+        mix = "preview mix: sides 128-256 squared, 1-8 spp"
+    else:
+        mix = (f"sides {'128-384' if args.small else '128-1024'} squared, 1-{64 if args.small else 256} spp")
     line = {
         "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, Rng of the reference)",
         "config": {"workload": f"served: {len(trace)} requests over {len(dev)} resident scenes (batched-workload "
-                               f"soups, unit Cornell box, caustic scene), sides "
-                               f"{'128-384' if args.small else '128-1024'} squared, 1-{64 if args.small else 256} spp, "
-                               f"depth 8, continuous batching of progressive passes (8 Mi paths per step, two steps "
-                               f"in flight), all requests queued at t=0",
+                               f"soups, unit Cornell box, caustic scene), {mix}, depth 8, continuous batching of "
+                               f"progressive passes (8 Mi paths per step, two steps in flight, round robin), all "
+                               f"requests queued at t=0",
                    "requests": len(trace), "scenes": len(dev), "samples_per_step": samples,
                    "server_steps": srv.steps, "peak_device_bytes": srv.peak_bytes,
                    "parallelism": f"replicas x{args.gpus}"},
@@ -780,7 +789,8 @@ def run_served(args, rank, world):
                              "what": "the same requests as consecutive ct_render_image_device calls, one at a time"},
         "speedup_vs_plain": value / plain_rate,
         "latency": {"arrivals": f"Poisson, {rate:.1f} requests/s (80% of the plain path's capacity)",
-                    "served": latency_stats(res_s), "plain": latency_stats(res_p), "served_steps": srv_s.steps},
+                    "served": latency_stats(res_s), "served_fifo": latency_stats(res_f), "plain": latency_stats(res_p),
+                    "served_steps": srv_s.steps},
         "clocks": clocks.summary(),
         "e2e": {"value": samples * args.steps * world / t_wall / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(sum(r.buffer_bytes for r in trace)),

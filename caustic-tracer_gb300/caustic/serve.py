@@ -90,9 +90,14 @@ class Executor(Protocol):
 
 
 class RenderServer:
+    POLICIES = ("round_robin", "fifo")
+
     def __init__(self, executor: Executor, budget_bytes: int = 120 << 30, step_paths: int = 8 << 20,
                  min_chunk_paths: int = 8 << 20, max_passes_per_step: Optional[int] = None,
-                 clock: Callable[[], float] = time.perf_counter):
+                 clock: Callable[[], float] = time.perf_counter, policy: str = "round_robin"):
+        if policy not in self.POLICIES:
+            raise ValueError(f"policy {policy!r} is not one of {self.POLICIES}")
+        self.policy = policy
         self.ex = executor
         self.budget = int(budget_bytes)
         self.step_paths = int(step_paths)
@@ -174,19 +179,23 @@ class RenderServer:
 
     # -- scheduling ------------------------------------------------------------
     def _plan(self) -> list:
-        """One step: requests with passes left, in round-robin order from where
-        the last step stopped, all of the first one's walk class, packed into
-        at most step_paths paths (one wave). Each gets an equal share of the
+        """One step: requests with passes left, all of the first one's walk
+        class, packed into at most step_paths paths (one wave). Order: round
+        robin from where the last step stopped (small requests finish within a
+        few steps of arriving; large ones share the GPU), or fifo: always from
+        the oldest (a large request runs as fast as alone, later ones only fill
+        what is left of each wave). Each request gets an equal share of the
         step, but at least min_chunk_paths (a request's chunk keeps its scene
         hot in L2 for a while) and at least one pass, at most what it still
         needs and what still fits; requests that do not fit wait for the next
-        step, which starts at the first of them."""
+        step, which under round robin starts at the first of them."""
         pending = [a for a in self.active if a.issued < a.req.spp and a.stop is None]
         if not pending:
             return []
         pending.sort(key=lambda a: a.seq)
-        k = next((i for i, a in enumerate(pending) if a.seq >= self._next), 0)
-        pending = pending[k:] + pending[:k]
+        if self.policy == "round_robin":
+            k = next((i for i, a in enumerate(pending) if a.seq >= self._next), 0)
+            pending = pending[k:] + pending[:k]
         cls = self.ex.walk_class(pending[0].req.scene)
         share = max(self.step_paths / len(pending), min(self.min_chunk, self.step_paths))
         room = self.step_paths

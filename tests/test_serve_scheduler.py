@@ -213,3 +213,16 @@ def test_cancel_waiting_and_in_flight_requests():
     assert issued0 < 9  # no passes launched after the cancel
     assert not any(rid == 3 for items in ex.steps for rid, _, _ in items)
     assert not ex.live
+
+
+def test_fifo_policy_runs_the_oldest_request_at_full_rate():
+    ex = FakeExecutor({"a": 0})
+    step_paths = 64 * 64 * 4
+    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=step_paths, clock=Clock(), policy="fifo")
+    srv.submit(_req(0, 64, 12))   # needs three full steps
+    srv.submit(_req(1, 16, 4))    # small: fills the leftover room of each wave
+    srv.drain()
+    steps_with_0 = [items for items in ex.steps if any(rid == 0 for rid, _, _ in items)]
+    assert len(steps_with_0) == 3 and all(dict((r, p) for r, _, p in s)[0] == 4 for s in steps_with_0)
+    with pytest.raises(ValueError):
+        RenderServer(ex, policy="lifo")
