@@ -15,6 +15,8 @@
 #include <new>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "scene.hpp"
 
 namespace ct {
@@ -248,6 +250,31 @@ void build_quads(const ct_packed_scene_view& v, std::vector<float4>& recs, int32
   *stack_need = need[0];
 }
 
+// The records as the walk reads them, 64 bytes each: the six bound arrays as
+// IEEE half floats, lower bounds rounded down and upper bounds rounded up
+// (each box only grows, so no box the reference enters is missed; empty slots
+// stay NaN), then the four child references:
+//   [0] lo.x[0..3] hi.x[0..3]  [1] lo.y hi.y  [2] lo.z hi.z  (half2 pairs)  [3] refs
+std::vector<uint4> half_records(const std::vector<float4>& recs) {
+  const size_t R = recs.size() / 8;
+  std::vector<uint4> out(R * 4);
+  auto pair = [](float a, float b, bool up) {
+    const __half ha = up ? __float2half_ru(a) : __float2half_rd(a);
+    const __half hb = up ? __float2half_ru(b) : __float2half_rd(b);
+    return (uint32_t)__half_as_ushort(ha) | ((uint32_t)__half_as_ushort(hb) << 16);
+  };
+  for (size_t r = 0; r < R; r++) {
+    const float4* q = &recs[r * 8];
+    for (int a = 0; a < 3; a++) {
+      const float4 lo = q[2 * a], hi = q[2 * a + 1];
+      out[r * 4 + a] = make_uint4(pair(lo.x, lo.y, false), pair(lo.z, lo.w, false), pair(hi.x, hi.y, true),
+                                  pair(hi.z, hi.w, true));
+    }
+    std::memcpy(&out[r * 4 + 3], &q[6], sizeof(uint4));
+  }
+  return out;
+}
+
 ct_status validate_view(const ct_packed_scene_view& v) {
   CT_CHECK_ARG(v.node_count == 0 || v.nodes != nullptr, "nodes is NULL");
   CT_CHECK_ARG(v.prim_count == 0 || v.prims != nullptr, "prims is NULL");
@@ -318,8 +345,10 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   std::vector<float4> quads;
   int32_t root_ref = ~0;
   uint32_t stack_need = 0;
+  std::vector<uint4> halves;
   try {
     build_quads(v, quads, &root_ref, &stack_need);
+    halves = half_records(quads);
   } catch (const std::bad_alloc&) {
     return fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");
   }
@@ -351,7 +380,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   s->sky = v.sky;
   if ((st = upload(s, s->prims, reinterpret_cast<const float4*>(v.prims), (size_t)v.prim_count * 4, 4)) != CT_OK ||
       (st = upload(s, s->nodes, reinterpret_cast<const float4*>(v.nodes), (size_t)v.node_count * 2, 2)) != CT_OK ||
-      (st = upload(s, s->quads, quads.data(), quads.size(), 8)) != CT_OK ||
+      (st = upload(s, s->quads, halves.data(), halves.size(), 4)) != CT_OK ||
       (st = upload(s, s->mats, reinterpret_cast<const float4*>(v.mats), (size_t)v.mat_count * 4, 4)) != CT_OK ||
       (st = upload(s, s->lights, v.lights, v.light_count, 1)) != CT_OK ||
       (st = upload(s, s->prim_object, v.prim_object, v.prim_count, 1)) != CT_OK ||
@@ -370,7 +399,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   ctk::SceneDev& d = s->dev;
   d.prims = s->prims.as<float4>();
   d.nodes = s->nodes.as<float4>();
-  d.quads = s->quads.as<float4>();
+  d.quads = s->quads.as<uint4>();
   d.mats = s->mats.as<float4>();
   d.lights = s->lights.as<int32_t>();
   d.prim_object = s->prim_object.as<uint32_t>();

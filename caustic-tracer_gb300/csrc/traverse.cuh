@@ -17,6 +17,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace ctk {
@@ -30,13 +31,13 @@ constexpr float kTRel = 4e-6f;
 constexpr float kBoxWiden = 1.0000005f;      // 1 + 2*gamma(3), rounded up
 
 // Device view of a scene. `quads` holds the reference BVH collapsed to four
-// children per record (128 bytes): lo.x, hi.x, lo.y, hi.y, lo.z, hi.z of the
-// four children (one float4 each; NaN for an empty slot), then the four child
-// references (>= 0 record, < 0 ~leafword).
+// children per record (64 bytes): the children's lo.x, hi.x, lo.y, hi.y,
+// lo.z, hi.z as half floats rounded outwards (NaN for an empty slot), then
+// the four child references (>= 0 record, < 0 ~leafword).
 struct SceneDev {
   const float4* __restrict__ prims;  // 4 per primitive (pack.ts:6-10)
   const float4* __restrict__ nodes;  // 2 per reference node (bvh.ts:6-15)
-  const float4* __restrict__ quads;  // 8 per 4-wide record
+  const uint4* __restrict__ quads;   // 4 per 4-wide record
   const float4* __restrict__ mats;   // 4 per material (pack.ts:12-16)
   const int32_t* __restrict__ lights;
   const uint32_t* __restrict__ prim_object;
@@ -491,15 +492,18 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
     }
     if (++w.cur == w.end) w.ref = kWalkPop;
   } else if (w.ref >= 0 && w.ref != kWalkPop) {
-    const float4* q = s.quads + (size_t)w.ref * 8;
-    const float4 xl = __ldg(q), xh = __ldg(q + 1), yl = __ldg(q + 2), yh = __ldg(q + 3);
-    const float4 zl = __ldg(q + 4), zh = __ldg(q + 5);
-    const int4 c4 = __ldg(reinterpret_cast<const int4*>(q + 6));
+    const uint4* q = s.quads + (size_t)w.ref * 4;
+    const uint4 bx = __ldg(q), by = __ldg(q + 1), bz = __ldg(q + 2);
+    const int4 c4 = __ldg(reinterpret_cast<const int4*>(q + 3));
+    auto f2 = [](uint32_t h) { return __half22float2(*reinterpret_cast<const __half2*>(&h)); };
+    const float2 xl01 = f2(bx.x), xl23 = f2(bx.y), xh01 = f2(bx.z), xh23 = f2(bx.w);
+    const float2 yl01 = f2(by.x), yl23 = f2(by.y), yh01 = f2(by.z), yh23 = f2(by.w);
+    const float2 zl01 = f2(bz.x), zl23 = f2(bz.y), zh01 = f2(bz.z), zh23 = f2(bz.w);
     const float bound = prune_bound(w.h);
-    float t0 = box_entry(w.r, xl.x, xh.x, yl.x, yh.x, zl.x, zh.x, bound);
-    float t1 = box_entry(w.r, xl.y, xh.y, yl.y, yh.y, zl.y, zh.y, bound);
-    float t2 = box_entry(w.r, xl.z, xh.z, yl.z, yh.z, zl.z, zh.z, bound);
-    float t3 = box_entry(w.r, xl.w, xh.w, yl.w, yh.w, zl.w, zh.w, bound);
+    float t0 = box_entry(w.r, xl01.x, xh01.x, yl01.x, yh01.x, zl01.x, zh01.x, bound);
+    float t1 = box_entry(w.r, xl01.y, xh01.y, yl01.y, yh01.y, zl01.y, zh01.y, bound);
+    float t2 = box_entry(w.r, xl23.x, xh23.x, yl23.x, yh23.x, zl23.x, zh23.x, bound);
+    float t3 = box_entry(w.r, xl23.y, xh23.y, yl23.y, yh23.y, zl23.y, zh23.y, bound);
     int32_t c0 = c4.x, c1 = c4.y, c2 = c4.z, c3 = c4.w;
     // Nearest first (misses, +inf, last): a five-exchange sorting network.
     auto order = [](float& ta, int32_t& ca, float& tb, int32_t& cb) {
