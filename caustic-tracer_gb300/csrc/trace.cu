@@ -21,12 +21,12 @@ namespace {
 
 std::atomic<int32_t> g_variant{0};  // 0 ordered short-stack walk, 1 stackless skip links
 
-// 12 blocks of 128 per SM (40 registers, a few spilled): the walk is a chain
+// 16 blocks of 128 per SM (32 registers, some spilled): the walk is a chain
 // of dependent loads and gains more from warps in flight than it loses to the
-// spills (1M-triangle soup: 683 Mrays/s, against 580 at 8 blocks and 614 at
-// 16, where the four-box step spills heavily).
+// spills (1M-triangle soup, 64-byte records: 759 Mrays/s against 749 at 12
+// blocks).
 template <int VARIANT, bool ANY>
-__global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
+__global__ void __launch_bounds__(128, 16) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
                                                uint32_t n, int32_t* __restrict__ prim,
                                                float* __restrict__ t_out, float* __restrict__ u_out,
                                                float* __restrict__ v_out,

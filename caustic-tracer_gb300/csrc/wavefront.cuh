@@ -214,12 +214,12 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
 enum WalkForm : int { kWalkThread = 0, kWalkPersistent = 1, kWalkSkip = 2, kWalkPerJob = 3 };
 
 // Closest hits of the bounce-b path queue plus the shadow rays of bounce b-1.
-// The ordered walks are latency-bound chains of dependent record loads, so
-// they are held to 40 registers (12 blocks = 1536 threads per SM; 32 registers
-// spill the four-box step and run slower, 64 halve the warps in flight); the
-// skip-link walk (small trees, short walks) keeps its registers.
+// Blocks of 128 per SM, measured per walk form: the ordered walk per thread
+// at 16 (32 registers), the persistent ordered walk at 12 (40 registers:
+// its refill state spills at 32; 925 vs 902 Msamples/s on the caustic
+// scene), the skip-link walk at 8 (it keeps its registers).
 template <int FORM>
-constexpr int trace_min_blocks() { return FORM == 2 ? 8 : 12; }
+constexpr int trace_min_blocks() { return FORM == 2 ? 8 : FORM == 1 ? 12 : 16; }
 
 template <int FORM, bool BATCH>
 __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(WaveArgs a, int32_t bounce) {
