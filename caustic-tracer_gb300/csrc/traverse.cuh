@@ -548,13 +548,14 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
 
 // Persistent warp loop over `total` queries numbered 0..total-1, handed out in
 // warp-sized batches from *counter. begin(i, w) loads query i into w.r and
-// calls walk_begin; finish(i, w) consumes the answer. A lane whose query is
-// answered is refilled as soon as a quarter of the warp is idle, so lanes
-// keep stepping instead of waiting for the warp's slowest ray. All 32 lanes
-// of every warp must call this (the block size is a multiple of 32).
+// calls walk_begin; finish(i, w) consumes the answer. Lanes whose queries are
+// answered are refilled as soon as REFILL lanes of the warp are idle, so
+// lanes keep stepping instead of waiting for the warp's slowest ray (8 suits
+// the exact query walk, 16 the integrator's: measured). All 32 lanes of every
+// warp must call this (the block size is a multiple of 32).
 // `s` is the scene the lane walks: a fixed scene, or (queries of many scenes)
 // a per-lane copy that begin() replaces with the new query's scene.
-template <bool EXACT, class Scene, class Begin, class Finish>
+template <bool EXACT, int REFILL, class Scene, class Begin, class Finish>
 __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uint32_t total, Begin begin,
                                                 Finish finish, uint32_t& fallbacks) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -570,7 +571,7 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
       idx = -1;
     }
     const uint32_t want = __ballot_sync(0xffffffffu, idle);
-    if (!drained && (__popc(want) >= 8 || want == 0xffffffffu)) {
+    if (!drained && (__popc(want) >= REFILL || want == 0xffffffffu)) {
       const uint32_t leader = __ffs(want) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(want));
