@@ -138,10 +138,15 @@ def occluded(scene: DeviceScene, rays: np.ndarray) -> np.ndarray:
     return out.astype(bool)
 
 
+TRAVERSALS = {"ordered": 0, "stackless": 1, "ordered_thread": 2}
+
+
 def set_traversal(variant: str) -> str:
-    """Selects the traversal kernel: 'ordered' (short stack) or 'stackless' (skip links)."""
-    prev = _native.lib().ct_set_traversal(1 if variant == "stackless" else 0)
-    return "stackless" if prev == 1 else "ordered"
+    """Selects the query kernel: 'ordered' (short stack, persistent lanes),
+    'stackless' (skip links) or 'ordered_thread' (short stack, one query per
+    thread). Returns the previous variant."""
+    prev = _native.lib().ct_set_traversal(TRAVERSALS[variant])
+    return {v: k for k, v in TRAVERSALS.items()}[prev]
 
 
 def accumulate_pass(scene: DeviceScene, frame: CameraFrame, width: int, height: int, frame_index: int,

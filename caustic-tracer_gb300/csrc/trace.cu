@@ -19,7 +19,8 @@ namespace ct {
 
 namespace {
 
-std::atomic<int32_t> g_variant{0};  // 0 ordered short-stack walk, 1 stackless skip links
+// 0 ordered walk (persistent lanes), 1 stackless skip links, 2 ordered walk one query per thread
+std::atomic<int32_t> g_variant{0};
 
 // 16 blocks of 128 per SM (32 registers, some spilled): the walk is a chain
 // of dependent loads and gains more from warps in flight than it loses to the
@@ -63,6 +64,16 @@ __global__ void __launch_bounds__(128, 16) k_trace(ctk::SceneDev s, const float4
           store(i, w.r, w.h);
         },
         fallbacks);
+  } else if (VARIANT == 2) {  // the ordered walk, one query per thread
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+      ctk::Walk w;
+      load(i, w.r);
+      ctk::walk_begin(s, w, ANY);
+      while (w.ref != ctk::kWalkDone) ctk::walk_step<true>(s, w, fallbacks);
+      overflow |= w.overflow;
+      store(i, w.r, w.h);
+    }
   } else {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -117,7 +128,8 @@ ct_status launch(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, floa
                  float* v, uint8_t* blocked, cudaStream_t stream) {
   if (n == 0) return CT_OK;
   // A tree whose walk could outgrow the ordered walk's stack uses the stackless walk.
-  const int variant = (g_variant.load() == 1 || s->stack_need > ctk::kStackSize) ? 1 : 0;
+  const int chosen = g_variant.load();
+  const int variant = (chosen == 1 || s->stack_need > ctk::kStackSize) ? 1 : chosen;
   const float4* r4 = reinterpret_cast<const float4*>(rays);
   uint32_t* cnt = s->counters.as<uint32_t>();
   CT_CUDA(cudaMemsetAsync(cnt + kCountQueue, 0, sizeof(uint32_t), stream));  // persistent work counter
@@ -125,6 +137,8 @@ ct_status launch(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, floa
     ProfScope ps(ANY ? "occluded" : "closest", stream);
     if (variant == 0)
       k_trace<0, ANY><<<grid_for<0, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+    else if (variant == 2)
+      k_trace<2, ANY><<<grid_for<2, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
     else
       k_trace<1, ANY><<<grid_for<1, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
   }
@@ -299,7 +313,7 @@ ct_status ct_pick(ct_scene* scene, const ct_camera_frame* frame, uint32_t count,
 }
 
 int32_t ct_set_traversal(int32_t variant) {
-  return ct::g_variant.exchange(variant == 1 ? 1 : 0);
+  return ct::g_variant.exchange(variant == 1 || variant == 2 ? variant : 0);
 }
 
 ct_status ct_trace_closest(ct_scene* scene, const float* rays, uint32_t count, int32_t* prim,

@@ -232,8 +232,9 @@ ct_status ct_trace_occluded_device(ct_scene* scene, const float* rays, uint32_t 
                                    uint8_t* blocked, void* stream);
 
 /* Traversal variant used by the query entry points:
- * 0 = ordered short-stack walk (near child first), 1 = stackless skip-link
- * walk (intersect.ts:290-365). Returns the previous value.                  */
+ * 0 = ordered short-stack walk (near child first) with persistent lane
+ * refill, 1 = stackless skip-link walk (intersect.ts:290-365), 2 = ordered
+ * walk, one query per thread. Returns the previous value.                  */
 int32_t ct_set_traversal(int32_t variant);
 
 /* ---- integrator ---------------------------------------------------------

@@ -38,7 +38,7 @@ def random_scene(native_lib):
         yield packed, dev
 
 
-@pytest.mark.parametrize("variant", ["ordered", "stackless"])
+@pytest.mark.parametrize("variant", ["ordered", "stackless", "ordered_thread"])
 def test_closest_matches_reference_rays(oracle, random_scene, variant):  # bvh.test.ts:88-112
     packed, dev = random_scene
     prev = ct.set_traversal(variant)
@@ -55,7 +55,7 @@ def test_closest_matches_reference_rays(oracle, random_scene, variant):  # bvh.t
         ct.set_traversal(prev)
 
 
-@pytest.mark.parametrize("variant", ["ordered", "stackless"])
+@pytest.mark.parametrize("variant", ["ordered", "stackless", "ordered_thread"])
 def test_closest_many_rays_and_finite_tmax(oracle, random_scene, variant):  # bvh.test.ts:114-131
     packed, dev = random_scene
     prev = ct.set_traversal(variant)
@@ -77,7 +77,7 @@ def test_closest_many_rays_and_finite_tmax(oracle, random_scene, variant):  # bv
         ct.set_traversal(prev)
 
 
-@pytest.mark.parametrize("variant", ["ordered", "stackless"])
+@pytest.mark.parametrize("variant", ["ordered", "stackless", "ordered_thread"])
 def test_occluded_matches_reference(oracle, random_scene, variant):  # bvh.test.ts:134-146
     packed, dev = random_scene
     prev = ct.set_traversal(variant)
