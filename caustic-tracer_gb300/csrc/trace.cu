@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "profile.hpp"
@@ -26,7 +27,9 @@ std::atomic<int32_t> g_variant{0};
 // of dependent loads and gains more from warps in flight than it loses to the
 // spills (1M-triangle soup, 64-byte records: 759 Mrays/s against 749 at 12
 // blocks).
-template <int VARIANT, bool ANY>
+// BARY: barycentrics are returned (u_out, v_out); otherwise the walk does
+// not carry them, which keeps two registers free per lane.
+template <int VARIANT, bool ANY, bool BARY>
 __global__ void __launch_bounds__(128, 16) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
                                                uint32_t n, int32_t* __restrict__ prim,
                                                float* __restrict__ t_out, float* __restrict__ u_out,
@@ -48,8 +51,8 @@ __global__ void __launch_bounds__(128, 16) k_trace(ctk::SceneDev s, const float4
     } else {
       prim[i] = h.prim;
       t_out[i] = h.prim < 0 ? INFINITY : (h.err > ctk::kReportRel * h.t ? -h.t : h.t);
-      if (u_out) u_out[i] = h.prim >= 0 ? h.u : 0.0f;
-      if (v_out) v_out[i] = h.prim >= 0 ? h.v : 0.0f;
+      if (BARY && u_out) u_out[i] = h.prim >= 0 ? h.u : 0.0f;
+      if (BARY && v_out) v_out[i] = h.prim >= 0 ? h.v : 0.0f;
     }
   };
   if (VARIANT == 0) {
@@ -108,14 +111,14 @@ __global__ void __launch_bounds__(256) k_refine(ctk::SceneDev s, const float4* _
   }
 }
 
-template <int VARIANT, bool ANY>
+template <int VARIANT, bool ANY, bool BARY>
 int grid_for(uint32_t n) {
   static int per_sm = -1, sms = 0;
   if (per_sm < 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<VARIANT, ANY>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<VARIANT, ANY, BARY>, 128, 0);
     if (per_sm < 1) per_sm = 1;
   }
   const uint64_t need = ((uint64_t)n + 127) / 128;
@@ -135,12 +138,20 @@ ct_status launch(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, floa
   CT_CUDA(cudaMemsetAsync(cnt + kCountQueue, 0, sizeof(uint32_t), stream));  // persistent work counter
   {
     ProfScope ps(ANY ? "occluded" : "closest", stream);
+    auto go = [&](auto variant_c, auto bary_c) {
+      constexpr int V = decltype(variant_c)::value;
+      constexpr bool B = decltype(bary_c)::value;
+      k_trace<V, ANY, B><<<grid_for<V, ANY, B>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+    };
+    using B0 = std::integral_constant<bool, false>;
+    using B1 = std::integral_constant<bool, true>;
+    const bool bary = !ANY && (u || v);
     if (variant == 0)
-      k_trace<0, ANY><<<grid_for<0, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+      bary ? go(std::integral_constant<int, 0>{}, B1{}) : go(std::integral_constant<int, 0>{}, B0{});
     else if (variant == 2)
-      k_trace<2, ANY><<<grid_for<2, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+      bary ? go(std::integral_constant<int, 2>{}, B1{}) : go(std::integral_constant<int, 2>{}, B0{});
     else
-      k_trace<1, ANY><<<grid_for<1, ANY>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+      bary ? go(std::integral_constant<int, 1>{}, B1{}) : go(std::integral_constant<int, 1>{}, B0{});
   }
   CT_CUDA(cudaGetLastError());
   if (!ANY) {
