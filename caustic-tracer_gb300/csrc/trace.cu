@@ -50,7 +50,12 @@ __global__ void __launch_bounds__(128, 16) k_trace(ctk::SceneDev s, const float4
       blocked[i] = h.prim >= 0 ? 1 : 0;
     } else {
       prim[i] = h.prim;
-      t_out[i] = h.prim < 0 ? INFINITY : (h.err > ctk::kReportRel * h.t ? -h.t : h.t);
+      float t = h.t;
+      bool loose = h.err > ctk::kReportRel * h.t;
+      // Without barycentrics, a loose triangle hit first tries the plane
+      // distance (float32, bounded); k_refine takes what is still loose.
+      if (!BARY && loose && h.prim >= 0 && ctk::plane_t(s, r, h.prim, ctk::kReportRel, t)) loose = false;
+      t_out[i] = h.prim < 0 ? INFINITY : (loose ? -h.t : t);
       if (BARY && u_out) u_out[i] = h.prim >= 0 ? h.u : 0.0f;
       if (BARY && v_out) v_out[i] = h.prim >= 0 ? h.v : 0.0f;
     }
@@ -101,6 +106,13 @@ __global__ void __launch_bounds__(256) k_refine(ctk::SceneDev s, const float4* _
     if (!(t_out[i] < 0.0f)) continue;
     const float4 r0 = __ldg(rays + 2 * (size_t)i), r1 = __ldg(rays + 2 * (size_t)i + 1);
     ctk::RayF r{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, 0.0f, 0.0f, 0.0f};
+    if (!u_out && !v_out) {  // only t is wanted: the plane distance in float64
+      const double tp = ctk::plane_t64(s, r, prim[i]);
+      if (tp > 0) {
+        t_out[i] = (float)tp;
+        continue;
+      }
+    }
     ctk::HitF h{prim[i], -t_out[i], 0.0f, 0.0f, 1.0f};
     if (u_out) h.u = u_out[i];
     if (v_out) h.v = v_out[i];

@@ -26,7 +26,7 @@ def check_closest(oracle, packed, rays, hits, label=""):
     hit = p >= 0
     if hit.any():
         rel = np.abs(hits.t[hit].astype(np.float64) - t[hit]) / t[hit]
-        assert rel.max() <= 5e-6, f"{label}: t relative error {rel.max()}"
+        assert rel.max() <= 4e-6, f"{label}: t relative error {rel.max()}"  # the reported bound, kTRel
     assert np.isinf(hits.t[~hit]).all()
     return len(diff), int(hit.sum())
 
