@@ -301,17 +301,50 @@ static __device__ __noinline__ void refine_hit(const SceneDev& s, const RayF& r,
   h.err = rounding_err(h.t);
 }
 
+// ---- double-float arithmetic (pairs hi + lo of floats, about 2^-44 per op) --
+// Error-free transformations with explicit fused multiply-adds: two_sum (Knuth)
+// and two_prod (fma), then renormalised sums and products.
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+  return F2{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ F2 quick_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return F2{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ F2 f2_add(F2 x, F2 y) {
+  const F2 s = two_sum(x.hi, y.hi);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ F2 f2_mul(F2 x, F2 y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  const float e = __fmaf_rn(x.hi, y.hi, -p);
+  return quick_two_sum(p, __fadd_rn(e, __fadd_rn(__fmul_rn(x.hi, y.lo), __fmul_rn(x.lo, y.hi))));
+}
+__device__ __forceinline__ F2 f2_neg(F2 x) { return F2{-x.hi, -x.lo}; }
+__device__ __forceinline__ F2 f2_div(F2 x, F2 y) {
+  const float q1 = __fdiv_rn(x.hi, y.hi);
+  const F2 r = f2_add(x, f2_neg(f2_mul(F2{q1, 0.0f}, y)));
+  return quick_two_sum(q1, __fdiv_rn(r.hi, y.hi));
+}
+
 // Distance to the plane of triangle `prim`, whose normal is computed here
 // from the packed float32 vertices (the triangle the reference tests): with
-// e1 = b - a, e2 = c - a, n = e1 x e2 and w = a - o, t = n.w / n.d in
-// float32. First-order bound: the edges' and n's rounding (4 eps of each
-// component's magnitude sum P), w's and the dot products' (4 and 3 eps of
-// the terms' magnitudes) and the division's (eps), scaled by 1 + 1e-3 for the
-// second-order terms (below 40 eps^2) and the rounding of the bound itself. Unlike the Moller-Trumbore
-// quotient, whose error grows with distance / triangle size, this one grows
-// only with the angles, so it serves as the reported t of a closest hit whose
-// walk bound is loose. Returns false for spheres or when the bound exceeds
-// `rel` (relative).
+// e1 = b - a, e2 = c - a, n = e1 x e2 and w = a - o, t = n.w / n.d. First
+// in float32 with a first-order bound: the edges' and n's rounding (4 eps of
+// each component's magnitude sum P), w's and the dot products' (4 and 3 eps
+// of the terms' magnitudes) and the division's (eps), scaled by 1 + 1e-3 for
+// the second-order terms (below 40 eps^2) and the bound's own rounding. When
+// that bound exceeds `rel`, the same formula in double-float arithmetic,
+// whose bound is the float32 one scaled by 2^-16 (a double-float operation
+// rounds at 2^-40 or better) plus the final rounding to float32. Unlike the
+// Moller-Trumbore quotient, whose error grows with distance / triangle size,
+// these grow only with the angles, so they serve as the reported t of a
+// closest hit whose walk bound is loose. Returns false for spheres or when
+// neither bound is within `rel` (relative).
 __device__ __forceinline__ bool plane_t(const SceneDev& s, const RayF& r, int32_t prim, float rel, float& t) {
   const float4* q = s.prims + (size_t)prim * 4;
   const float4 a4 = __ldg(q);
@@ -335,8 +368,22 @@ __device__ __forceinline__ bool plane_t(const SceneDev& s, const RayF& r, int32_
   const float an = fabsf(num) - en, ad = fabsf(den) - ed;
   if (!(an > 0.0f && ad > 0.0f)) return false;
   const float bound = 1.001f * (en / an + ed / ad + kEps);
-  if (!(bound <= rel)) return false;
-  t = num / den;
+  if (bound <= rel) {
+    t = num / den;
+    return t > 0.0f;
+  }
+  if (!(bound * 0x1p-16f + 2.0f * kEps <= rel)) return false;
+  // Double-float: the edge and w differences of floats are exact as pairs.
+  const F2 E1x = two_sum(b4.x, -a4.x), E1y = two_sum(b4.y, -a4.y), E1z = two_sum(b4.z, -a4.z);
+  const F2 E2x = two_sum(c4.x, -a4.x), E2y = two_sum(c4.y, -a4.y), E2z = two_sum(c4.z, -a4.z);
+  const F2 Wx = two_sum(a4.x, -r.ox), Wy = two_sum(a4.y, -r.oy), Wz = two_sum(a4.z, -r.oz);
+  const F2 Nx = f2_add(f2_mul(E1y, E2z), f2_neg(f2_mul(E1z, E2y)));
+  const F2 Ny = f2_add(f2_mul(E1z, E2x), f2_neg(f2_mul(E1x, E2z)));
+  const F2 Nz = f2_add(f2_mul(E1x, E2y), f2_neg(f2_mul(E1y, E2x)));
+  const F2 Num = f2_add(f2_add(f2_mul(Nx, Wx), f2_mul(Ny, Wy)), f2_mul(Nz, Wz));
+  const F2 Den = f2_add(f2_add(f2_mul(Nx, F2{r.dx, 0.0f}), f2_mul(Ny, F2{r.dy, 0.0f})), f2_mul(Nz, F2{r.dz, 0.0f}));
+  const F2 T = f2_div(Num, Den);
+  t = T.hi;
   return t > 0.0f;
 }
 
