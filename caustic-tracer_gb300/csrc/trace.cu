@@ -23,14 +23,14 @@ namespace {
 // 0 ordered walk (persistent lanes), 1 stackless skip links, 2 ordered walk one query per thread
 std::atomic<int32_t> g_variant{0};
 
-// 16 blocks of 128 per SM (32 registers, some spilled): the walk is a chain
-// of dependent loads and gains more from warps in flight than it loses to the
-// spills (1M-triangle soup, 64-byte records: 759 Mrays/s against 749 at 12
-// blocks).
+// 12 blocks of 128 per SM (40 registers, some spilled): the walk is a chain
+// of dependent loads and gains from warps in flight, while fewer threads keep
+// its local memory (state, stack) closer to L1 (1M-triangle soup: 837 Mrays/s
+// against 834 at 16 blocks and about 20 % fewer DRAM bytes).
 // BARY: barycentrics are returned (u_out, v_out); otherwise the walk does
 // not carry them, which keeps two registers free per lane.
 template <int VARIANT, bool ANY, bool BARY>
-__global__ void __launch_bounds__(128, 16) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
+__global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4* __restrict__ rays,
                                                uint32_t n, int32_t* __restrict__ prim,
                                                float* __restrict__ t_out, float* __restrict__ u_out,
                                                float* __restrict__ v_out,
