@@ -26,7 +26,7 @@ std::atomic<int32_t> g_variant{0};
 // 12 blocks of 128 per SM (40 registers, some spilled): the walk is a chain
 // of dependent loads and gains from warps in flight, while fewer threads keep
 // its local memory (state, stack) closer to L1 (1M-triangle soup: 837 Mrays/s
-// against 834 at 16 blocks and about 20 % fewer DRAM bytes).
+// against 834 at 16 blocks).
 // BARY: barycentrics are returned (u_out, v_out); otherwise the walk does
 // not carry them, which keeps two registers free per lane.
 template <int VARIANT, bool ANY, bool BARY>
