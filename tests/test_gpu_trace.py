@@ -131,3 +131,46 @@ def test_ragged_batch_sizes(oracle, random_scene):
         if n:
             check_closest(oracle, packed, rays_all[:n], hits, f"n={n}")
 
+
+
+def _grazing_case(offset, n=60_000, seed=31):
+    """Large, thin and small triangles around `offset`, hit by rays that graze
+    them (direction nearly in the triangles' plane) and by ordinary rays."""
+    from caustic.scene import Lambertian, Mesh, Scene, SceneObject
+
+    rng = np.random.default_rng(seed)
+    tris = []
+    for k in range(400):
+        size = 10.0 ** rng.uniform(-3, 1)
+        centre = offset + rng.uniform(-5, 5, 3)
+        e1 = rng.normal(size=3)
+        e2 = rng.normal(size=3) * (10.0 ** rng.uniform(-3, 0))  # some thin triangles
+        tris.append([centre, centre + size * e1, centre + size * e2])
+    verts = np.asarray(tris, np.float64).reshape(-1, 3)
+    mesh = Mesh(verts, np.arange(len(verts), dtype=np.uint32))
+    scene = Scene("grazing", [SceneObject("m", "m", mesh, Lambertian((0.5, 0.5, 0.5)))], ct.CORNELL_BOX.camera)
+    packed = ct.pack_scene(scene)
+    pick = rng.integers(0, len(tris), n)
+    t = np.asarray(tris)[pick]
+    bary = rng.dirichlet((1, 1, 1), n)
+    target = (bary[:, :, None] * t).sum(1)
+    normal = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0])
+    normal /= np.linalg.norm(normal, axis=1, keepdims=True)
+    inplane = np.cross(normal, rng.normal(size=(n, 3)))
+    inplane /= np.linalg.norm(inplane, axis=1, keepdims=True)
+    tilt = 10.0 ** rng.uniform(-5, 0, n)[:, None]  # cos(angle to the plane) from 1e-5 to 1
+    d = inplane * np.sqrt(1 - tilt ** 2) + normal * tilt
+    dist = 10.0 ** rng.uniform(-1, 2, n)[:, None]
+    origin = target - d * dist
+    return packed, ct.make_rays(origin.astype(np.float32), d.astype(np.float32))
+
+
+@pytest.mark.parametrize("offset", [0.0, 3000.0])
+def test_reported_distance_bound_holds_on_grazing_and_far_geometry(oracle, native_lib, offset):
+    packed, rays = _grazing_case(np.array([offset, -offset / 3, offset / 7]))
+    with ct.DeviceScene(packed) as dev:
+        hits = ct.intersect_closest(dev, rays)
+        ties, n_hit = check_closest(oracle, packed, rays, hits, f"grazing@{offset}")
+        assert n_hit > 0.5 * len(rays)
+        with_bary = ct.intersect_closest(dev, rays, barycentrics=True)  # the float64 refine path
+        check_closest(oracle, packed, rays, with_bary, f"grazing@{offset}+uv")
