@@ -55,6 +55,15 @@ namespace {
 std::mutex g_pool_mu;
 constexpr int kPoolDevices = 64;
 cudaMemPool_t g_pool[kPoolDevices] = {};
+
+// Idle scene streams and their timing events, kept per device so that scene
+// create and destroy do not pay for stream and event creation each time.
+struct StreamSet {
+  cudaStream_t stream;
+  cudaEvent_t ev0, ev1, ev2;
+};
+constexpr size_t kIdleStreams = 32;
+std::vector<StreamSet> g_idle[kPoolDevices];
 }  // namespace
 
 ct_status path_pool(int device, cudaMemPool_t* out) {
@@ -307,11 +316,17 @@ ct_status validate_view(const ct_packed_scene_view& v) {
   return CT_OK;
 }
 
+// The scene's arrays share one allocation from the per-device stream-ordered
+// pool (scene create and destroy then cost no cudaMalloc / cudaFree, and the
+// latter would wait for the whole device).
+size_t arena_slot(size_t bytes) { return (bytes + 255) & ~size_t(255); }
+
 template <class T>
-ct_status upload(ct_scene* s, DeviceBuffer& b, const T* src, size_t count, size_t min_count) {
+ct_status upload(ct_scene* s, DeviceBuffer& b, char*& cursor, const T* src, size_t count, size_t min_count) {
   const size_t n = count > min_count ? count : min_count;
-  ct_status st = b.reserve(n * sizeof(T), &s->device_bytes);
-  if (st != CT_OK) return st;
+  b.ptr = cursor;
+  b.bytes = n * sizeof(T);
+  cursor += arena_slot(b.bytes);
   CT_CUDA(cudaMemsetAsync(b.ptr, 0, n * sizeof(T), s->stream));
   if (count) CT_CUDA(cudaMemcpyAsync(b.ptr, src, count * sizeof(T), cudaMemcpyHostToDevice, s->stream));
   return CT_OK;
@@ -323,13 +338,29 @@ void destroy(ct_scene* s) {
   cudaGetDevice(&prev);
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
-  for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->quads, &s->mats, &s->lights, &s->prim_object, &s->io,
-                          &s->counters})
-    b->release(&s->device_bytes);
-  if (s->ev0) cudaEventDestroy(s->ev0);
-  if (s->ev1) cudaEventDestroy(s->ev1);
-  if (s->ev2) cudaEventDestroy(s->ev2);
-  if (s->stream) cudaStreamDestroy(s->stream);
+  for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->quads, &s->mats, &s->lights, &s->prim_object, &s->counters})
+    b->ptr = nullptr, b->bytes = 0;  // slices of the arena
+  if (s->arena) path_free(s->arena, s->stream);
+  s->io.release(&s->device_bytes);
+  bool kept = false;
+  if (s->stream && s->ev0 && s->ev1 && s->ev2 && s->device >= 0 && s->device < kPoolDevices &&
+      cudaStreamSynchronize(s->stream) == cudaSuccess) {
+    std::lock_guard<std::mutex> guard(g_pool_mu);
+    std::vector<StreamSet>& idle = g_idle[s->device];
+    if (idle.size() < kIdleStreams) {
+      try {
+        idle.push_back({s->stream, s->ev0, s->ev1, s->ev2});
+        kept = true;
+      } catch (const std::bad_alloc&) {
+      }
+    }
+  }
+  if (!kept) {
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->ev2) cudaEventDestroy(s->ev2);
+    if (s->stream) cudaStreamDestroy(s->stream);
+  }
   cudaSetDevice(prev);
   delete s;
 }
@@ -360,7 +391,16 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
     destroy(s);
     return code;
   };
-  {
+  if (s->device >= 0 && s->device < kPoolDevices) {
+    std::lock_guard<std::mutex> guard(g_pool_mu);
+    std::vector<StreamSet>& idle = g_idle[s->device];
+    if (!idle.empty()) {
+      const StreamSet set = idle.back();
+      idle.pop_back();
+      s->stream = set.stream, s->ev0 = set.ev0, s->ev1 = set.ev1, s->ev2 = set.ev2;
+    }
+  }
+  if (!s->stream) {
     cudaError_t err = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (err != cudaSuccess) {
       s->stream = nullptr;
@@ -378,13 +418,23 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   s->depth = depth;
   s->stack_need = stack_need;
   s->sky = v.sky;
-  if ((st = upload(s, s->prims, reinterpret_cast<const float4*>(v.prims), (size_t)v.prim_count * 4, 4)) != CT_OK ||
-      (st = upload(s, s->nodes, reinterpret_cast<const float4*>(v.nodes), (size_t)v.node_count * 2, 2)) != CT_OK ||
-      (st = upload(s, s->quads, halves.data(), halves.size(), 4)) != CT_OK ||
-      (st = upload(s, s->mats, reinterpret_cast<const float4*>(v.mats), (size_t)v.mat_count * 4, 4)) != CT_OK ||
-      (st = upload(s, s->lights, v.lights, v.light_count, 1)) != CT_OK ||
-      (st = upload(s, s->prim_object, v.prim_object, v.prim_count, 1)) != CT_OK ||
-      (st = s->counters.reserve(kCounterWords * sizeof(uint32_t), &s->device_bytes)) != CT_OK)
+  const size_t arena = arena_slot(std::max<size_t>(v.prim_count * 4, 4) * sizeof(float4)) +
+                       arena_slot(std::max<size_t>(v.node_count * 2, 2) * sizeof(float4)) +
+                       arena_slot(std::max<size_t>(halves.size(), 4) * sizeof(uint4)) +
+                       arena_slot(std::max<size_t>(v.mat_count * 4, 4) * sizeof(float4)) +
+                       arena_slot(std::max<size_t>(v.light_count, 1) * sizeof(int32_t)) +
+                       arena_slot(std::max<size_t>(v.prim_count, 1) * sizeof(uint32_t)) +
+                       arena_slot(kCounterWords * sizeof(uint32_t));
+  if ((st = path_alloc(s->device, arena, s->stream, &s->arena)) != CT_OK) return bail(st);
+  s->device_bytes += arena;
+  char* cursor = static_cast<char*>(s->arena);
+  if ((st = upload(s, s->prims, cursor, reinterpret_cast<const float4*>(v.prims), (size_t)v.prim_count * 4, 4)) != CT_OK ||
+      (st = upload(s, s->nodes, cursor, reinterpret_cast<const float4*>(v.nodes), (size_t)v.node_count * 2, 2)) != CT_OK ||
+      (st = upload(s, s->quads, cursor, halves.data(), halves.size(), 4)) != CT_OK ||
+      (st = upload(s, s->mats, cursor, reinterpret_cast<const float4*>(v.mats), (size_t)v.mat_count * 4, 4)) != CT_OK ||
+      (st = upload(s, s->lights, cursor, v.lights, v.light_count, 1)) != CT_OK ||
+      (st = upload(s, s->prim_object, cursor, v.prim_object, v.prim_count, 1)) != CT_OK ||
+      (st = upload(s, s->counters, cursor, (const uint32_t*)nullptr, 0, kCounterWords)) != CT_OK)
     return bail(st);
   if (v.mat_count == 0 && v.mats != nullptr) {
     // The reference always allocates one material record (pack.ts:122).

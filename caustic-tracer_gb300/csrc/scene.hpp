@@ -52,7 +52,9 @@ struct ct_scene {
   cudaStream_t stream = nullptr;
   std::mutex lock;
 
-  // Device copies of the packed arrays plus the 4-wide walk records.
+  // Device copies of the packed arrays plus the 4-wide walk records: slices
+  // of one pool allocation (`arena`).
+  void* arena = nullptr;
   ct::DeviceBuffer prims, nodes, quads, mats, lights, prim_object;
   uint32_t prim_count = 0, node_count = 0, interior_count = 0, mat_count = 0, light_count = 0;
   uint32_t depth = 0;       // deepest root-to-leaf path, in nodes

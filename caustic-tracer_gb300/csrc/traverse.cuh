@@ -553,8 +553,7 @@ struct Walk {
   uint32_t cur, end;
   int32_t sp;
   bool any, overflow;
-  int32_t stack_ref[kStackSize];
-  float stack_t[kStackSize];
+  int2 stack[kStackSize];  // (child reference, entry distance bits): one 8-byte access per push or pop
 };
 
 constexpr int32_t kWalkPop = INT32_MAX, kWalkDone = INT32_MIN, kWalkLeaf = INT32_MIN + 1;
@@ -633,9 +632,9 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
       w.ref = kWalkDone;
       return;
     } else {
-      if (hits > 3) w.stack_ref[w.sp] = c3, w.stack_t[w.sp++] = t3;
-      if (hits > 2) w.stack_ref[w.sp] = c2, w.stack_t[w.sp++] = t2;
-      if (hits > 1) w.stack_ref[w.sp] = c1, w.stack_t[w.sp++] = t1;
+      if (hits > 3) w.stack[w.sp++] = make_int2(c3, __float_as_int(t3));
+      if (hits > 2) w.stack[w.sp++] = make_int2(c2, __float_as_int(t2));
+      if (hits > 1) w.stack[w.sp++] = make_int2(c1, __float_as_int(t1));
       walk_enter(w, c0);
     }
   }
@@ -644,8 +643,9 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
     const float bound = prune_bound(w.h);
     while (w.sp > 0) {
       --w.sp;
-      if (w.stack_t[w.sp] <= bound) {
-        walk_enter(w, w.stack_ref[w.sp]);
+      const int2 e = w.stack[w.sp];
+      if (__int_as_float(e.y) <= bound) {
+        walk_enter(w, e.x);
         break;
       }
     }
@@ -657,11 +657,18 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
 // calls walk_begin; finish(i, w) consumes the answer. Lanes whose queries are
 // answered are refilled as soon as REFILL lanes of the warp are idle, so
 // lanes keep stepping instead of waiting for the warp's slowest ray (8 suits
-// the exact query walk, 16 the integrator's: measured). All 32 lanes of every
-// warp must call this (the block size is a multiple of 32).
+// the exact query walk, 16 the integrator's: measured). Each round of the
+// loop takes two steps per lane, which halves the refill bookkeeping (one
+// step per round ran 5 % slower on the 1M-triangle query walk, three or four
+// 20-35 % slower). With PHASED, the second step of a round moves either the
+// lanes testing primitives or those expanding records, whichever are more, so each branch
+// runs with fuller warps; every lane still makes its own tests in the same
+// order (measured: 1.5 % faster for the integrator's walk, 4 % slower for the
+// exact query walk). All 32 lanes of every warp must call this (the block
+// size is a multiple of 32).
 // `s` is the scene the lane walks: a fixed scene, or (queries of many scenes)
 // a per-lane copy that begin() replaces with the new query's scene.
-template <bool EXACT, int REFILL, class Scene, class Begin, class Finish>
+template <bool EXACT, int REFILL, bool PHASED, class Scene, class Begin, class Finish>
 __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uint32_t total, Begin begin,
                                                 Finish finish, uint32_t& fallbacks) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -693,6 +700,13 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
     }
     if (__all_sync(0xffffffffu, idx < 0) && drained) break;
     if (w.ref != kWalkDone) walk_step<EXACT>(s, w, fallbacks);
+    bool go = w.ref != kWalkDone;
+    if (PHASED) {
+      const uint32_t leaf = __ballot_sync(0xffffffffu, w.ref == kWalkLeaf);
+      const uint32_t inner = __ballot_sync(0xffffffffu, w.ref >= 0);
+      go = go && (w.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
+    }
+    if (go) walk_step<EXACT>(s, w, fallbacks);
   }
 }
 

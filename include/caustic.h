@@ -192,6 +192,9 @@ uint32_t ct_rng_stream(uint32_t seed_or_state, int32_t is_state, uint64_t n, int
  * Replaces the implicit "arrays are readable" contract of the reference's
  * tracer (tracer.ts:348, intersect.ts:202).                                 */
 ct_status ct_scene_create(const ct_packed_scene_view* ps, ct_scene** out);
+/* Waits for the scene's own stream and returns its arrays (one allocation
+ * from the per-device pool) to the pool. Batches that read the scene must be
+ * finished or destroyed first (ct_batch_destroy waits for its run).       */
 void ct_scene_destroy(ct_scene* scene);
 /* Device bytes held by the scene (for admission budgets). Path state of a
  * render or batch is not part of it: it comes from a per-device
