@@ -628,6 +628,20 @@ def run_batched(args, rank, world):
             _native.check(lib.ct_render_image_device(j.scene.handle, C.byref(f), C.byref(o), _native.ptr(out),
                                                      C.c_void_p(stream.cuda_stream)))
 
+    topts = opts.struct()
+    spp_div = torch.full((), float(spp), dtype=torch.float32, device=device)  # true division, as renderImage
+
+    def per_frame_step():
+        # each job as a progressive loop: one accumulatePass per frame, then / spp
+        with torch.cuda.stream(stream):
+            for j, f, out in zip(jobs, fstructs, outs):
+                out.zero_()
+                for k in range(spp):
+                    _native.check(lib.ct_accumulate_passes_device(
+                        j.scene.handle, C.byref(f), j.width, j.height, (j.seed * 7919 + k) & 0xFFFFFFFF, 1,
+                        C.byref(topts), _native.ptr(out), None, C.c_void_p(stream.cuda_stream)))
+                out.div_(spp_div)
+
     def timed(step, steps):
         with torch.cuda.stream(stream):
             for _ in range(max(3, args.warmup)):
@@ -646,6 +660,8 @@ def run_batched(args, rank, world):
         t_batch = timed(batched_step, args.steps)
     t_plain = timed(plain_step, max(1, args.steps // 2))
     plain_rate = samples * max(1, args.steps // 2) * world / t_plain / 1e6
+    t_frame = timed(per_frame_step, 1)
+    frame_rate = samples * world / t_frame / 1e6
     value = samples * args.steps * world / t_batch / 1e6
     # end to end: graph launch + copy of every job's sums to the host
     t0 = time.perf_counter()
@@ -668,6 +684,10 @@ def run_batched(args, rank, world):
         "plain_sequential": {"value": plain_rate, "unit": "Msamples/s",
                              "what": "the same jobs as consecutive ct_render_image_device calls"},
         "speedup_vs_plain": value / plain_rate,
+        "plain_per_frame": {"value": frame_rate, "unit": "Msamples/s",
+                            "what": "the same jobs one after another, each as a progressive loop of one "
+                                    "accumulatePass per frame (ct_accumulate_passes_device, passes = 1)"},
+        "speedup_vs_per_frame": value / frame_rate,
         "clocks": clocks.summary(),
         "e2e": {"value": e2e_rate, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(sum(j.width * j.height * 12 for j in jobs)),
@@ -714,7 +734,7 @@ def run_served(args, rank, world):
     import torch
 
     import caustic as ct
-    from caustic.serve import GpuExecutor, RenderServer, latency_stats, render_plain
+    from caustic.serve import GpuExecutor, RenderServer, latency_stats, render_per_frame, render_plain
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     device = torch.device("cuda", torch.cuda.current_device())
@@ -748,6 +768,12 @@ def run_served(args, rank, world):
         torch.cuda.synchronize()
         return res, time.perf_counter() - t0
 
+    def per_frame(rate=None):
+        t0 = time.perf_counter()
+        res = render_per_frame(dev, at(trace, rate), opts, t0=t0)
+        torch.cuda.synchronize()
+        return res, time.perf_counter() - t0
+
     for _ in range(max(3, args.warmup)):
         served()
     plain()
@@ -765,6 +791,9 @@ def run_served(args, rank, world):
     t_plain = max_over_ranks(t_plain, world, device)
     value = samples * args.steps * world / t_dev / 1e6
     plain_rate = samples * world / t_plain / 1e6
+    _, t_frame = per_frame()
+    t_frame = max_over_ranks(t_frame, world, device)
+    frame_rate = samples * world / t_frame / 1e6
     # latency under Poisson arrivals at 80% of the plain path's request capacity
     rate = 0.8 * len(trace) / t_plain
     res_s, _, _, srv_s = served(rate)
@@ -788,6 +817,10 @@ def run_served(args, rank, world):
         "plain_sequential": {"value": plain_rate, "unit": "Msamples/s",
                              "what": "the same requests as consecutive ct_render_image_device calls, one at a time"},
         "speedup_vs_plain": value / plain_rate,
+        "plain_per_frame": {"value": frame_rate, "unit": "Msamples/s",
+                            "what": "the same requests one at a time, each as a progressive loop of one "
+                                    "accumulatePass per frame (ct_accumulate_passes_device, passes = 1)"},
+        "speedup_vs_per_frame": value / frame_rate,
         "latency": {"arrivals": f"Poisson, {rate:.1f} requests/s (80% of the plain path's capacity)",
                     "served": latency_stats(res_s), "served_fifo": latency_stats(res_f), "plain": latency_stats(res_p),
                     "served_steps": srv_s.steps},

@@ -409,6 +409,47 @@ def render_plain(scenes: Dict[str, DeviceScene], requests: Sequence[Request], op
     return results
 
 
+def render_per_frame(scenes: Dict[str, DeviceScene], requests: Sequence[Request], opts: TraceOptions,
+                     clock: Callable[[], float] = time.perf_counter, t0: Optional[float] = None) -> List[Result]:
+    """The per-frame baseline: requests served one at a time in arrival order,
+    each as the reference's progressive loop renders it, one accumulatePass
+    (ct_accumulate_passes_device with passes = 1) per frame with frame index
+    seed*7919 + k (tracer.ts:351), then divided by spp. The frames are
+    queued back to back on one stream; the host waits once per request."""
+    import ctypes as C
+
+    import torch
+
+    from . import _native
+
+    lib = _native.lib()
+    stream = torch.cuda.Stream()
+    t0 = clock() if t0 is None else t0
+    o = opts.struct()
+    results = []
+    for req in sorted(requests, key=lambda r: r.arrival):
+        arrival = t0 + req.arrival
+        while clock() < arrival:
+            time.sleep(max(0.0, min(0.01, arrival - clock())))
+        start = clock()
+        f = req.frame.struct()
+        with torch.cuda.stream(stream):
+            accum = torch.zeros(req.pixels * 3, dtype=torch.float32, device="cuda")
+            for k in range(req.spp):
+                _native.check(lib.ct_accumulate_passes_device(
+                    scenes[req.scene].handle, C.byref(f), req.width, req.height,
+                    (req.seed * 7919 + k) & 0xFFFFFFFF, 1, C.byref(o), _native.ptr(accum), None,
+                    C.c_void_p(stream.cuda_stream)))
+            # a device divisor: torch turns division by a host scalar into a
+            # multiply by its reciprocal, which is not the division renderImage does
+            accum.div_(torch.full((), float(req.spp), dtype=torch.float32, device="cuda"))
+        stream.synchronize()
+        img = accum.cpu().numpy()
+        r = Request(req.rid, req.scene, req.frame, req.width, req.height, req.spp, req.seed, arrival)
+        results.append(Result(r, img, start, clock()))
+    return results
+
+
 def poisson_requests(names: Sequence[str], frames: Dict[str, Callable[[float], CameraFrame]], count: int,
                      rate: float, seed: int = 99, sides=(128, 256, 384, 512, 768, 1024), max_spp: int = 256):
     """`count` requests with exponential inter-arrival times of mean 1/rate: a

@@ -98,3 +98,17 @@ def test_run_direct_equals_graph_run(device_scenes):
         sums.append([b.cpu().numpy() for b in bufs])
     for a, b in zip(*sums):
         assert np.array_equal(a, b)
+
+
+def test_per_frame_baseline_equals_plain(device_scenes):
+    """The per-frame baseline (one accumulatePass per frame) and the plain
+    renderImage baseline produce the same images: they differ in launch
+    pattern only, which is what the served bench compares against."""
+    from caustic.serve import render_per_frame, render_plain
+
+    scenes, dev = device_scenes
+    reqs = _requests(scenes)[:5]
+    plain = {r.request.rid: r.image for r in render_plain(dev, reqs, OPTS)}
+    frames = {r.request.rid: r.image for r in render_per_frame(dev, reqs, OPTS)}
+    for r in reqs:
+        assert np.array_equal(plain[r.rid], frames[r.rid]), r
