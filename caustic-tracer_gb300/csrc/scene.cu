@@ -284,6 +284,51 @@ std::vector<uint4> half_records(const std::vector<float4>& recs) {
   return out;
 }
 
+// Plane records of the integrator's primitive tests, 48 bytes per primitive
+// (Havel and Herout, "Yet Faster Ray-Triangle Intersection (Using SSE4)",
+// IEEE TVCG 16(3), 2010). For a triangle (a, b, c) with n = (b-a) x (c-a):
+//   [0] n, n.a   [1] n1 = ((c-a) x n) / |n|^2, -n1.a   [2] n2 = (n x (b-a)) / |n|^2, -n2.a
+// so that n1.(p-a) and n2.(p-a) are the barycentric weights of b and c (the
+// reference's u and v) of a point p in the plane. Computed in float64 and
+// rounded once. A degenerate triangle (n = 0) gets zero records, which the
+// test rejects as parallel. A sphere: [0] centre, radius  [1] NaN marker.
+std::vector<float4> plane_records(const ct_packed_scene_view& v) {
+  std::vector<float4> out((size_t)v.prim_count * 3);
+  for (uint32_t p = 0; p < v.prim_count; p++) {
+    const float* q = v.prims + (size_t)p * CT_PRIM_STRIDE;
+    float4* o = &out[(size_t)p * 3];
+    if (q[3] == CT_PRIM_SPHERE) {
+      o[0] = make_float4(q[0], q[1], q[2], q[4]);
+      o[1] = make_float4(NAN, 0.0f, 0.0f, 0.0f);
+      o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      continue;
+    }
+    const double a[3] = {q[0], q[1], q[2]};
+    const double e1[3] = {(double)q[4] - a[0], (double)q[5] - a[1], (double)q[6] - a[2]};
+    const double e2[3] = {(double)q[8] - a[0], (double)q[9] - a[1], (double)q[10] - a[2]};
+    auto cross = [](const double* x, const double* y, double* z) {
+      z[0] = x[1] * y[2] - x[2] * y[1];
+      z[1] = x[2] * y[0] - x[0] * y[2];
+      z[2] = x[0] * y[1] - x[1] * y[0];
+    };
+    auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+    double n[3], n1[3], n2[3];
+    cross(e1, e2, n);
+    const double l2 = dot(n, n);
+    if (!(l2 > 0.0) || !std::isfinite(l2)) {
+      o[0] = o[1] = o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      continue;
+    }
+    cross(e2, n, n1);
+    cross(n, e1, n2);
+    for (int k = 0; k < 3; k++) n1[k] /= l2, n2[k] /= l2;
+    o[0] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)dot(n, a));
+    o[1] = make_float4((float)n1[0], (float)n1[1], (float)n1[2], (float)-dot(n1, a));
+    o[2] = make_float4((float)n2[0], (float)n2[1], (float)n2[2], (float)-dot(n2, a));
+  }
+  return out;
+}
+
 ct_status validate_view(const ct_packed_scene_view& v) {
   CT_CHECK_ARG(v.node_count == 0 || v.nodes != nullptr, "nodes is NULL");
   CT_CHECK_ARG(v.prim_count == 0 || v.prims != nullptr, "prims is NULL");
@@ -338,7 +383,8 @@ void destroy(ct_scene* s) {
   cudaGetDevice(&prev);
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
-  for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->quads, &s->mats, &s->lights, &s->prim_object, &s->counters})
+  for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->quads, &s->mats, &s->lights, &s->prim_object, &s->planes,
+                          &s->counters})
     b->ptr = nullptr, b->bytes = 0;  // slices of the arena
   if (s->arena) path_free(s->arena, s->stream);
   s->io.release(&s->device_bytes);
@@ -377,9 +423,11 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   int32_t root_ref = ~0;
   uint32_t stack_need = 0;
   std::vector<uint4> halves;
+  std::vector<float4> planes;
   try {
     build_quads(v, quads, &root_ref, &stack_need);
     halves = half_records(quads);
+    planes = plane_records(v);
   } catch (const std::bad_alloc&) {
     return fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");
   }
@@ -424,6 +472,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
                        arena_slot(std::max<size_t>(v.mat_count * 4, 4) * sizeof(float4)) +
                        arena_slot(std::max<size_t>(v.light_count, 1) * sizeof(int32_t)) +
                        arena_slot(std::max<size_t>(v.prim_count, 1) * sizeof(uint32_t)) +
+                       arena_slot(std::max<size_t>(planes.size(), 3) * sizeof(float4)) +
                        arena_slot(kCounterWords * sizeof(uint32_t));
   if ((st = path_alloc(s->device, arena, s->stream, &s->arena)) != CT_OK) return bail(st);
   s->device_bytes += arena;
@@ -434,6 +483,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
       (st = upload(s, s->mats, cursor, reinterpret_cast<const float4*>(v.mats), (size_t)v.mat_count * 4, 4)) != CT_OK ||
       (st = upload(s, s->lights, cursor, v.lights, v.light_count, 1)) != CT_OK ||
       (st = upload(s, s->prim_object, cursor, v.prim_object, v.prim_count, 1)) != CT_OK ||
+      (st = upload(s, s->planes, cursor, planes.data(), planes.size(), 3)) != CT_OK ||
       (st = upload(s, s->counters, cursor, (const uint32_t*)nullptr, 0, kCounterWords)) != CT_OK)
     return bail(st);
   if (v.mat_count == 0 && v.mats != nullptr) {
@@ -450,6 +500,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   d.prims = s->prims.as<float4>();
   d.nodes = s->nodes.as<float4>();
   d.quads = s->quads.as<uint4>();
+  d.planes = s->planes.as<float4>();
   d.mats = s->mats.as<float4>();
   d.lights = s->lights.as<int32_t>();
   d.prim_object = s->prim_object.as<uint32_t>();

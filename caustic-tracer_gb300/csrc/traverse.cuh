@@ -38,6 +38,7 @@ struct SceneDev {
   const float4* __restrict__ prims;  // 4 per primitive (pack.ts:6-10)
   const float4* __restrict__ nodes;  // 2 per reference node (bvh.ts:6-15)
   const uint4* __restrict__ quads;   // 4 per 4-wide record
+  const float4* __restrict__ planes; // 3 per primitive: plane records of the float32 tests
   const float4* __restrict__ mats;   // 4 per material (pack.ts:12-16)
   const int32_t* __restrict__ lights;
   const uint32_t* __restrict__ prim_object;
@@ -394,36 +395,35 @@ __device__ __forceinline__ bool plane_t(const SceneDev& s, const RayF& r, int32_
 // 19 ms launch on the 1M-triangle soup.)
 constexpr float kReportRel = kTRel;
 
-// Plain float32 forms of the reference's tests (same decisions, float32
-// rounding), for the path integrator whose parity is statistical. The
-// candidate must also be nearer than `closest`. Every fused multiply-add is
+// Plain float32 tests for the path integrator, whose parity is statistical:
+// the reference's decisions (|det| < 1e-12 rejected, u, v in [0, 1],
+// u + v <= 1, t in (tmin, closest); near root then far root for spheres) in
+// float32, triangles in the plane-record form below. Every fused multiply-add is
 // written out (the library is compiled with -fmad=false), so each kernel
 // that inlines these tests rounds them identically.
 __device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
 
-// Division-free until a hit is certain: u, v and t are compared as
-// numerators against |det| (one reciprocal per accepted candidate instead of
-// one per test).
-__device__ __forceinline__ bool tri_fast(const RayF& r, float4 a4, float4 b4, float4 c4, float closest, Cand& c) {
-  const float e1x = b4.x - a4.x, e1y = b4.y - a4.y, e1z = b4.z - a4.z;
-  const float e2x = c4.x - a4.x, e2y = c4.y - a4.y, e2z = c4.z - a4.z;
-  const float px = fm(r.dy, e2z, -mul(r.dz, e2y));
-  const float py = fm(r.dz, e2x, -mul(r.dx, e2z));
-  const float pz = fm(r.dx, e2y, -mul(r.dy, e2x));
-  const float det = fm(e1x, px, fm(e1y, py, mul(e1z, pz)));
+// Havel-Herout form on the plane records (p0 = n, n.a; p1 = n1, -n1.a;
+// p2 = n2, -n2.a): det = d.n (the reference's det with the sign flipped,
+// same magnitude for its |det| < 1e-12 rejection), t*det = n.(a - o), then
+// u*det and v*det from the hit point scaled by det, all compared as
+// numerators against |det|. The plane distance is tested first, before the
+// barycentrics.
+__device__ __forceinline__ bool tri_plane(const RayF& r, float4 p0, float4 p1, float4 p2, float closest, Cand& c) {
+  const float det = fm(r.dx, p0.x, fm(r.dy, p0.y, mul(r.dz, p0.z)));
   if (det > -1e-12f && det < 1e-12f) return false;
+  const float tn = p0.w - fm(r.ox, p0.x, fm(r.oy, p0.y, mul(r.oz, p0.z)));  // t * det
   const float ad = fabsf(det), sg = det < 0.0f ? -1.0f : 1.0f;
-  const float tx = r.ox - a4.x, ty = r.oy - a4.y, tz = r.oz - a4.z;
-  const float su = sg * fm(tx, px, fm(ty, py, mul(tz, pz)));  // u * |det|
-  if (su < 0.0f || su > ad) return false;
-  const float qx = fm(ty, e1z, -mul(tz, e1y));
-  const float qy = fm(tz, e1x, -mul(tx, e1z));
-  const float qz = fm(tx, e1y, -mul(ty, e1x));
-  const float sv = sg * fm(r.dx, qx, fm(r.dy, qy, mul(r.dz, qz)));  // v * |det|
-  if (sv < 0.0f || su + sv > ad) return false;
-  const float st = sg * fm(e2x, qx, fm(e2y, qy, mul(e2z, qz)));  // t * |det|
+  const float st = sg * tn;  // t * |det|
   if (st <= r.tmin * ad || st >= closest * ad) return false;
+  const float px = fm(r.ox, det, mul(r.dx, tn));  // det * (o + t d)
+  const float py = fm(r.oy, det, mul(r.dy, tn));
+  const float pz = fm(r.oz, det, mul(r.dz, tn));
+  const float su = sg * fm(p1.x, px, fm(p1.y, py, fm(p1.z, pz, mul(det, p1.w))));  // u * |det|
+  if (su < 0.0f || su > ad) return false;
+  const float sv = sg * fm(p2.x, px, fm(p2.y, py, fm(p2.z, pz, mul(det, p2.w))));  // v * |det|
+  if (sv < 0.0f || su + sv > ad) return false;
   const float inv = 1.0f / ad;
   const float t = st * inv;
   if (t <= r.tmin || t >= closest) return false;
@@ -464,12 +464,12 @@ __device__ __forceinline__ bool sphere_fast(const RayF& r, float4 c4, float rad,
 template <bool EXACT>
 __device__ __forceinline__ bool test_prim(const SceneDev& s, const RayF& r, uint32_t p, HitF& h, bool any,
                                           uint32_t& fallbacks) {
-  const float4* q = s.prims + (size_t)p * 4;
-  const float4 a4 = __ldg(q);
-  const float4 b4 = __ldg(q + 1);
   Cand c;
   if constexpr (!EXACT) {
-    const bool hit = a4.w == 0.0f ? sphere_fast(r, a4, b4.x, h.t, c) : tri_fast(r, a4, b4, __ldg(q + 2), h.t, c);
+    const float4* q = s.planes + (size_t)p * 3;
+    const float4 p0 = __ldg(q);
+    const float4 p1 = __ldg(q + 1);
+    const bool hit = p1.x != p1.x ? sphere_fast(r, p0, p0.w, h.t, c) : tri_plane(r, p0, p1, __ldg(q + 2), h.t, c);
     if (!hit) return false;
     h.prim = (int32_t)p;
     h.t = c.t;
@@ -477,6 +477,9 @@ __device__ __forceinline__ bool test_prim(const SceneDev& s, const RayF& r, uint
     h.v = c.v;
     return any;
   }
+  const float4* q = s.prims + (size_t)p * 4;
+  const float4 a4 = __ldg(q);
+  const float4 b4 = __ldg(q + 1);
   const bool cand = a4.w == 0.0f ? sphere_candidate(r, a4, b4.x, c, fallbacks)
                                  : tri_candidate(r, a4, b4, __ldg(q + 2), c, fallbacks);
   if (!cand) return false;
