@@ -266,17 +266,23 @@ def kernel_bytes_per_step(kernel: str, cpu: dict, units_per_step: int):
     48 B per triangle test, 32 B per sphere test (the reference's ordered walk).
     Shading: per closest-hit ray, 16 B hit + 32 B ray in, 48 B primitive +
     64 B material read, 32 B continuation ray out, plus 44 B per shadow ray out.
-    Accumulation: 12 B read + 12 B written per sample.
+    Accumulation: 12 B read + 12 B written per sample. Whole paths (k_paths,
+    scenes of at most 32 primitives): the ray-query and shading bytes of the
+    path together, plus its 16 B radiance written.
     """
     if "bytes_per_unit" in cpu:  # traversal workload: one closest-hit query per unit
         return cpu["bytes_per_unit"] * units_per_step if kernel == "closest" else None
     w = cpu["work_per_sample"]
+    trace = (w["closest_rays"] * (RAY_BYTES + HIT_BYTES) + w["shadow_rays"] * RAY_BYTES +
+             BOX_BYTES * (w["closest_aabb"] + w["shadow_aabb"]) + TRI_BYTES * (w["closest_tri"] + w["shadow_tri"]) +
+             SPHERE_BYTES * (w["closest_sphere"] + w["shadow_sphere"]))
+    shade = w["closest_rays"] * (16 + 32 + 48 + 64 + 32) + w["shadow_rays"] * 44
     if kernel == "trace":
-        per = (w["closest_rays"] * (RAY_BYTES + HIT_BYTES) + w["shadow_rays"] * RAY_BYTES +
-               BOX_BYTES * (w["closest_aabb"] + w["shadow_aabb"]) + TRI_BYTES * (w["closest_tri"] + w["shadow_tri"]) +
-               SPHERE_BYTES * (w["closest_sphere"] + w["shadow_sphere"]))
+        per = trace
     elif kernel == "shade":
-        per = w["closest_rays"] * (16 + 32 + 48 + 64 + 32) + w["shadow_rays"] * 44
+        per = shade
+    elif kernel == "paths":
+        per = trace + shade + 16
     elif kernel == "accumulate":
         per = 2 * ACCUM_BYTES_PER_SAMPLE
     else:
@@ -476,7 +482,10 @@ def kernel_profile(lib, dev, step, stream, args):
 
 def compulsory_bytes_per_step(kernel: str, cpu: dict, units_per_step: int):
     """Bytes a trace step must move at least: each ray read (32 B) and each
-    closest hit written (16 B); the scene once per launch is added by the caller."""
+    closest hit written (16 B); for whole paths (k_paths) each path's 16 B
+    radiance written. The scene once per launch is added by the caller."""
+    if kernel == "paths":
+        return units_per_step * 16
     if kernel not in ("trace", "closest"):
         return None
     if "bytes_per_unit" in cpu:
@@ -501,7 +510,7 @@ def roofline(args, prof, cpu, units_per_step, peak, peak_kind, scene_bytes=0):
     comp_step = compulsory_bytes_per_step(name, cpu, units_per_step) if cpu else None
     comp = comp_step / launches_per_step + scene_bytes if comp_step else None
     rec = traffic_record(args.workload + ("_small" if args.small else ""))
-    traffic = rec.get("dram_bytes_per_launch") if rec else None
+    traffic = rec.get("dram_bytes_per_launch") if rec and rec.get("scope") == name else None
     achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
     rate = lambda b: b / (avg_ms / 1e3) / 1e9 / peak if b else None  # noqa: E731
     out = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -18,6 +18,15 @@ from .camera import CameraFrame
 from .tracer import DeviceScene, TraceOptions
 
 
+def divide_exact(sums, n: int):
+    """sums / n in IEEE float32 division, as renderImage's final scale does.
+    (torch turns division by a host scalar into a multiply by its rounded
+    reciprocal, which can differ in the last bit.)"""
+    import torch
+
+    return sums / torch.full((), float(n), dtype=sums.dtype, device=sums.device)
+
+
 @dataclass
 class Job:
     scene: DeviceScene
@@ -70,7 +79,7 @@ class BatchRenderer:
         import torch
 
         torch.cuda.synchronize()
-        return [(a / j.spp).cpu().numpy() for a, j in zip(self.accums, self.jobs)]
+        return [divide_exact(a, j.spp).cpu().numpy() for a, j in zip(self.accums, self.jobs)]
 
     def info(self) -> dict:
         waves, nodes, walk = C.c_uint32(), C.c_uint64(), C.c_int32()

@@ -368,8 +368,10 @@ class GpuExecutor:
     def fetch(self, req: Request, buf) -> np.ndarray:
         import torch
 
+        from .batch import divide_exact
+
         with torch.cuda.stream(self.copy_stream):
-            out = (buf / req.spp).cpu()
+            out = divide_exact(buf, req.spp).cpu()
         return out.numpy()
 
     def release(self, buf) -> None:
@@ -421,6 +423,7 @@ def render_per_frame(scenes: Dict[str, DeviceScene], requests: Sequence[Request]
     import torch
 
     from . import _native
+    from .batch import divide_exact
 
     lib = _native.lib()
     stream = torch.cuda.Stream()
@@ -440,9 +443,7 @@ def render_per_frame(scenes: Dict[str, DeviceScene], requests: Sequence[Request]
                     scenes[req.scene].handle, C.byref(f), req.width, req.height,
                     (req.seed * 7919 + k) & 0xFFFFFFFF, 1, C.byref(o), _native.ptr(accum), None,
                     C.c_void_p(stream.cuda_stream)))
-            # a device divisor: torch turns division by a host scalar into a
-            # multiply by its reciprocal, which is not the division renderImage does
-            accum.div_(torch.full((), float(req.spp), dtype=torch.float32, device="cuda"))
+            accum = divide_exact(accum, req.spp)
         stream.synchronize()
         img = accum.cpu().numpy()
         r = Request(req.rid, req.scene, req.frame, req.width, req.height, req.spp, req.seed, arrival)

@@ -77,6 +77,25 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   a.nee = o.nee;
   const Grids<false>& g = grids<false>();
   const int form = walk_form(s);
+  if (form == kWalkSkip && s->prim_count <= ctk::kBrutePrims) {
+    // Whole paths per lane (k_paths): same sums, no path queues.
+    for (uint64_t done = 0; done < passes; done += per_wave) {
+      const uint32_t p = (uint32_t)std::min<uint64_t>(per_wave, passes - done);
+      a.paths = (uint32_t)(p * pixels);
+      a.first_frame = first + (uint32_t)done;
+      CT_CUDA(cudaMemsetAsync(a.counts, 0, counter_words * 4, stream));
+      {
+        ProfScope ps("paths", stream);
+        k_paths<<<g.paths, kBlock, 0, stream>>>(a);
+      }
+      {
+        ProfScope ps("accumulate", stream);
+        k_accumulate<<<g.acc, kBlock, 0, stream>>>(a.radiance, a.pixels, p, accum, sumsq);
+      }
+      CT_CUDA(cudaGetLastError());
+    }
+    return CT_OK;
+  }
   auto trace = [&](const WaveArgs& w, int32_t b) {
     ProfScope ps("trace", stream);
     launch_trace<false>(form, w, b, stream);

@@ -151,6 +151,34 @@ __device__ __forceinline__ uint32_t find_segment(const SegDev* segs, uint32_t ns
   return lo;
 }
 
+// The camera ray of one path (accumulatePass per pixel, tracer.ts:361-395):
+// jitter, optional lens sample and camera_ray, from Rng.fromPixel(pixel,
+// frame_index); the path's queue state (a, b, c) with unit throughput.
+__device__ __forceinline__ void generate_path(const ctk::FrameF& frame, uint32_t width, uint32_t height,
+                                              uint32_t pixel, uint32_t frame_index, uint32_t pid, float4& qa,
+                                              float4& qb, float4& qc) {
+  const uint32_t y = pixel / width, x = pixel - y * width;
+  uint32_t rng = ctk::seed_for(pixel, frame_index);
+  const float jx = ctk::next_f(rng);
+  const float jy = ctk::next_f(rng);
+  const float sx = ((float)x + jx) / (float)width;
+  const float sy = 1.0f - ((float)y + jy) / (float)height;
+  float lx = 0.0f, ly = 0.0f;
+  if (frame.lens_radius > 0.0f) {
+    const float r = sqrtf(ctk::next_f(rng));
+    float sp, cp;
+    sincospif(2.0f * ctk::next_f(rng), &sp, &cp);
+    lx = r * cp;
+    ly = r * sp;
+  }
+  ctk::V3f o, d;
+  ctk::camera_ray(frame, sx, sy, lx, ly, o, d);
+  qa = make_float4(o.x, o.y, o.z, __uint_as_float(rng));
+  qb = make_float4(d.x, d.y, d.z, -1.0f);
+  qc = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pid));
+}
+
+
 template <bool BATCH>
 __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -176,25 +204,11 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
       height = a.height;
       frame = &a.frame;
     }
-    const uint32_t y = pixel / width, x = pixel - y * width;
-    uint32_t rng = ctk::seed_for(pixel, frame_index);
-    const float jx = ctk::next_f(rng);
-    const float jy = ctk::next_f(rng);
-    const float sx = ((float)x + jx) / (float)width;
-    const float sy = 1.0f - ((float)y + jy) / (float)height;
-    float lx = 0.0f, ly = 0.0f;
-    if (frame->lens_radius > 0.0f) {
-      const float r = sqrtf(ctk::next_f(rng));
-      float sp, cp;
-      sincospif(2.0f * ctk::next_f(rng), &sp, &cp);
-      lx = r * cp;
-      ly = r * sp;
-    }
-    ctk::V3f o, d;
-    ctk::camera_ray(*frame, sx, sy, lx, ly, o, d);
-    a.cur.a[p] = make_float4(o.x, o.y, o.z, __uint_as_float(rng));
-    a.cur.b[p] = make_float4(d.x, d.y, d.z, -1.0f);
-    a.cur.c[p] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(p));
+    float4 qa, qb, qc;
+    generate_path(*frame, width, height, pixel, frame_index, p, qa, qb, qc);
+    a.cur.a[p] = qa;
+    a.cur.b[p] = qb;
+    a.cur.c[p] = qc;
     a.radiance[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) a.counts[0] = a.paths;
@@ -299,6 +313,123 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
   if (fallbacks) atomicAdd(a.counts + 2 * a.max_bounces + 6, fallbacks);
 }
 
+// Result of shading one path-bounce: the continuing path's state (cont),
+// the NEE shadow ray and its contribution (shadow), and the radiance
+// (emission or sky) to add to the path now.
+struct ShadeOut {
+  bool cont, shadow;
+  float4 na, nb, nc, sa, sb, scol;
+  float lr, lg, lb;
+};
+
+// One bounce of radianceInto (tracer.ts:191-328) for a path whose closest
+// hit is (prim, t) (prim < 0: miss): emission with its MIS weight, the
+// material's scatter (Lambertian with NEE, metal, dielectric), Russian
+// roulette. k_shade and the brute-force path kernel both run it, so the two
+// take the same float operations in the same order.
+__device__ __forceinline__ void shade_path(const ctk::SceneDev& sc, const SkyF& sky, uint32_t job, float4 qa,
+                                           float4 qb, float4 qc, int32_t prim, float t, int32_t bounce,
+                                           int32_t max_bounces, int32_t rr, int32_t nee, ShadeOut& out) {
+  out.cont = out.shadow = false;
+  out.na = out.nb = out.nc = out.sa = out.sb = out.scol = make_float4(0, 0, 0, 0);
+  out.lr = out.lg = out.lb = 0.0f;
+  const bool use_nee = nee != 0 && sc.light_count > 0;
+  uint32_t rng = __float_as_uint(qa.w);
+  const uint32_t pid = __float_as_uint(qc.w);
+  const ctk::V3f o = ctk::mk(qa.x, qa.y, qa.z), d = ctk::mk(qb.x, qb.y, qb.z);
+  float pdf = qb.w;
+  float tr = qc.x, tg = qc.y, tb = qc.z;
+  if (prim < 0) {
+    if (sky.kind == 1) {  // tracer.ts:210-218
+      const float f = 0.5f * (d.y + 1.0f);
+      out.lr = tr * (sky.horizon[0] + (sky.zenith[0] - sky.horizon[0]) * f) * sky.strength;
+      out.lg = tg * (sky.horizon[1] + (sky.zenith[1] - sky.horizon[1]) * f) * sky.strength;
+      out.lb = tb * (sky.horizon[2] + (sky.zenith[2] - sky.horizon[2]) * f) * sky.strength;
+    }
+  } else {
+    const float4* q = sc.prims + (size_t)prim * 4;
+    const float4 q0 = __ldg(q);
+    const ctk::V3f p = ctk::madd3(o, d, t);
+    ctk::V3f nrm;
+    if (q0.w == 0.0f) {
+      const float inv_r = 1.0f / __ldg(q + 1).x;
+      nrm = ctk::mk((p.x - q0.x) * inv_r, (p.y - q0.y) * inv_r, (p.z - q0.z) * inv_r);
+    } else {
+      const float4 q3 = __ldg(q + 3);
+      nrm = ctk::mk(q3.x, q3.y, q3.z);
+    }
+    const bool front = ctk::dot3(d, nrm) < 0.0f;
+    const ctk::V3f s = front ? nrm : ctk::mk(-nrm.x, -nrm.y, -nrm.z);
+    const float4* m = sc.mats + (size_t)__ldg(sc.prim_object + prim) * 4;
+    const float4 m0 = __ldg(m), m3 = __ldg(m + 3);
+    if (m3.x > 0.0f || m3.y > 0.0f || m3.z > 0.0f) {  // tracer.ts:243-252
+      float w = 1.0f;
+      if (use_nee && pdf >= 0.0f) w = ctk::power_heuristic(pdf, ctk::light_pdf(sc, o, p, nrm, prim));
+      out.lr = tr * m3.x * w;
+      out.lg = tg * m3.y * w;
+      out.lb = tb * m3.z * w;
+    }
+    const int type = (int)m0.w;
+    ctk::V3f nd = d;
+    if (type == CT_MAT_LAMBERTIAN) {
+      const float4 m1 = __ldg(m + 1);
+      float ar = m0.x, ag = m0.y, ab = m0.z;
+      if (m1.z > 0.5f && !ctk::checker_primary(p, m1.y)) {
+        const float4 m2 = __ldg(m + 2);
+        ar = m2.x, ag = m2.y, ab = m2.z;
+      }
+      ctk::LightSample ls;
+      if (use_nee && ctk::sample_light(sc, p, rng, ls)) {  // tracer.ts:263-274
+        const float cos_s = ctk::dot3(s, ls.dir);
+        if (cos_s > 0.0f && ls.pdf > 0.0f) {
+          const float pdf_b = cos_s * ctk::kInvPi;
+          const float k = (cos_s * ctk::kInvPi * ctk::power_heuristic(ls.pdf, pdf_b)) / ls.pdf;
+          out.shadow = true;
+          out.sa = make_float4(p.x, p.y, p.z, ls.dist * ctk::kShadowShorten);
+          out.sb = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, __uint_as_float(pid));
+          out.scol = make_float4(tr * ar * ls.emission.x * k, tg * ag * ls.emission.y * k,
+                                 tb * ab * ls.emission.z * k, __uint_as_float(job));
+        }
+      }
+      const float u1 = ctk::next_f(rng);
+      const float u2 = ctk::next_f(rng);
+      nd = ctk::cosine_hemisphere(s, u1, u2);
+      pdf = fmaxf(0.0f, ctk::dot3(s, nd)) * ctk::kInvPi;
+      tr *= ar, tg *= ag, tb *= ab;
+      out.cont = true;
+    } else if (type == CT_MAT_METAL) {
+      const float u1 = ctk::next_f(rng);
+      const float u2 = ctk::next_f(rng);
+      const float u3 = ctk::next_f(rng);
+      nd = ctk::metal_dir(d, s, __ldg(m + 1).x, u1, u2, u3);
+      if (ctk::dot3(nd, s) > 0.0f) {
+        tr *= m0.x, tg *= m0.y, tb *= m0.z;
+        pdf = -1.0f;
+        out.cont = true;
+      }
+    } else if (type == CT_MAT_DIELECTRIC) {
+      const float u = ctk::next_f(rng);
+      nd = ctk::dielectric_dir(d, s, __ldg(m + 1).x, front, u);
+      tr *= m0.x, tg *= m0.y, tb *= m0.z;
+      pdf = -1.0f;
+      out.cont = true;
+    }
+    if (out.cont && rr && bounce >= 3) {  // tracer.ts:305-312
+      const float max_b = fmaxf(tr, fmaxf(tg, tb));
+      const float ps = max_b > 1.0f ? 1.0f : (max_b < 0.05f ? 0.05f : max_b);
+      if (ctk::next_f(rng) > ps) {
+        out.cont = false;
+      } else {
+        tr /= ps, tg /= ps, tb /= ps;
+      }
+    }
+    if (bounce >= max_bounces) out.cont = false;
+    out.na = make_float4(p.x, p.y, p.z, __uint_as_float(rng));
+    out.nb = make_float4(nd.x, nd.y, nd.z, pdf);
+    out.nc = make_float4(tr, tg, tb, __uint_as_float(pid));
+  }
+}
+
 // 10 blocks of 128 per SM (48 registers, ~50 bytes spilled): 3 % faster on
 // the Cornell box than 8 blocks at 64 registers.
 template <bool BATCH>
@@ -319,105 +450,15 @@ __global__ void __launch_bounds__(kBlock, 10) k_shade(WaveArgs a, int32_t bounce
         sky = &a.jobs[job].sky;
       }
       const ctk::SceneDev sc = BATCH ? a.jobs[job].scene : a.scene;  // registers, loaded up front
-      const bool use_nee = a.nee != 0 && sc.light_count > 0;
       const float4 qa = a.cur.a[i], qb = a.cur.b[i], qc = a.cur.c[i];
-      uint32_t rng = __float_as_uint(qa.w);
-      const uint32_t pid = __float_as_uint(qc.w);
-      const ctk::V3f o = ctk::mk(qa.x, qa.y, qa.z), d = ctk::mk(qb.x, qb.y, qb.z);
-      float pdf = qb.w;
-      float tr = qc.x, tg = qc.y, tb = qc.z;
-      float lr = 0.0f, lg = 0.0f, lb = 0.0f;
       const int32_t prim = a.hit_prim[i];
-      if (prim < 0) {
-        if (sky->kind == 1) {  // tracer.ts:210-218
-          const float t = 0.5f * (d.y + 1.0f);
-          lr = tr * (sky->horizon[0] + (sky->zenith[0] - sky->horizon[0]) * t) * sky->strength;
-          lg = tg * (sky->horizon[1] + (sky->zenith[1] - sky->horizon[1]) * t) * sky->strength;
-          lb = tb * (sky->horizon[2] + (sky->zenith[2] - sky->horizon[2]) * t) * sky->strength;
-        }
-      } else {
-        const float t = a.hit_t[i];
-        const float4* q = sc.prims + (size_t)prim * 4;
-        const float4 q0 = __ldg(q);
-        const ctk::V3f p = ctk::madd3(o, d, t);
-        ctk::V3f nrm;
-        if (q0.w == 0.0f) {
-          const float inv_r = 1.0f / __ldg(q + 1).x;
-          nrm = ctk::mk((p.x - q0.x) * inv_r, (p.y - q0.y) * inv_r, (p.z - q0.z) * inv_r);
-        } else {
-          const float4 q3 = __ldg(q + 3);
-          nrm = ctk::mk(q3.x, q3.y, q3.z);
-        }
-        const bool front = ctk::dot3(d, nrm) < 0.0f;
-        const ctk::V3f s = front ? nrm : ctk::mk(-nrm.x, -nrm.y, -nrm.z);
-        const float4* m = sc.mats + (size_t)__ldg(sc.prim_object + prim) * 4;
-        const float4 m0 = __ldg(m), m3 = __ldg(m + 3);
-        if (m3.x > 0.0f || m3.y > 0.0f || m3.z > 0.0f) {  // tracer.ts:243-252
-          float w = 1.0f;
-          if (use_nee && pdf >= 0.0f) w = ctk::power_heuristic(pdf, ctk::light_pdf(sc, o, p, nrm, prim));
-          lr = tr * m3.x * w;
-          lg = tg * m3.y * w;
-          lb = tb * m3.z * w;
-        }
-        const int type = (int)m0.w;
-        ctk::V3f nd = d;
-        if (type == CT_MAT_LAMBERTIAN) {
-          const float4 m1 = __ldg(m + 1);
-          float ar = m0.x, ag = m0.y, ab = m0.z;
-          if (m1.z > 0.5f && !ctk::checker_primary(p, m1.y)) {
-            const float4 m2 = __ldg(m + 2);
-            ar = m2.x, ag = m2.y, ab = m2.z;
-          }
-          ctk::LightSample ls;
-          if (use_nee && ctk::sample_light(sc, p, rng, ls)) {  // tracer.ts:263-274
-            const float cos_s = ctk::dot3(s, ls.dir);
-            if (cos_s > 0.0f && ls.pdf > 0.0f) {
-              const float pdf_b = cos_s * ctk::kInvPi;
-              const float k = (cos_s * ctk::kInvPi * ctk::power_heuristic(ls.pdf, pdf_b)) / ls.pdf;
-              shadow = true;
-              sa = make_float4(p.x, p.y, p.z, ls.dist * ctk::kShadowShorten);
-              sb = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, __uint_as_float(pid));
-              scol = make_float4(tr * ar * ls.emission.x * k, tg * ag * ls.emission.y * k,
-                                 tb * ab * ls.emission.z * k, __uint_as_float(job));
-            }
-          }
-          const float u1 = ctk::next_f(rng);
-          const float u2 = ctk::next_f(rng);
-          nd = ctk::cosine_hemisphere(s, u1, u2);
-          pdf = fmaxf(0.0f, ctk::dot3(s, nd)) * ctk::kInvPi;
-          tr *= ar, tg *= ag, tb *= ab;
-          cont = true;
-        } else if (type == CT_MAT_METAL) {
-          const float u1 = ctk::next_f(rng);
-          const float u2 = ctk::next_f(rng);
-          const float u3 = ctk::next_f(rng);
-          nd = ctk::metal_dir(d, s, __ldg(m + 1).x, u1, u2, u3);
-          if (ctk::dot3(nd, s) > 0.0f) {
-            tr *= m0.x, tg *= m0.y, tb *= m0.z;
-            pdf = -1.0f;
-            cont = true;
-          }
-        } else if (type == CT_MAT_DIELECTRIC) {
-          const float u = ctk::next_f(rng);
-          nd = ctk::dielectric_dir(d, s, __ldg(m + 1).x, front, u);
-          tr *= m0.x, tg *= m0.y, tb *= m0.z;
-          pdf = -1.0f;
-          cont = true;
-        }
-        if (cont && a.rr && bounce >= 3) {  // tracer.ts:305-312
-          const float max_b = fmaxf(tr, fmaxf(tg, tb));
-          const float ps = max_b > 1.0f ? 1.0f : (max_b < 0.05f ? 0.05f : max_b);
-          if (ctk::next_f(rng) > ps) {
-            cont = false;
-          } else {
-            tr /= ps, tg /= ps, tb /= ps;
-          }
-        }
-        if (bounce >= a.max_bounces) cont = false;
-        na = make_float4(p.x, p.y, p.z, __uint_as_float(rng));
-        nb = make_float4(nd.x, nd.y, nd.z, pdf);
-        nc = make_float4(tr, tg, tb, __uint_as_float(pid));
-      }
+      const float t = prim >= 0 ? a.hit_t[i] : 0.0f;
+      ShadeOut so;
+      shade_path(sc, *sky, job, qa, qb, qc, prim, t, bounce, a.max_bounces, a.rr, a.nee, so);
+      cont = so.cont, shadow = so.shadow;
+      na = so.na, nb = so.nb, nc = so.nc, sa = so.sa, sb = so.sb, scol = so.scol;
+      const float lr = so.lr, lg = so.lg, lb = so.lb;
+      const uint32_t pid = __float_as_uint(qc.w);
       if (lr != 0.0f || lg != 0.0f || lb != 0.0f) {
         float4* L = a.radiance + pid;
         float4 l = *L;
@@ -439,6 +480,73 @@ __global__ void __launch_bounds__(kBlock, 10) k_shade(WaveArgs a, int32_t bounce
       a.shadow.a[sslot] = sa;
       a.shadow.b[sslot] = sb;
       a.shadow.c[sslot] = scol;
+    }
+  }
+}
+
+// Whole paths of a single scene of at most kBrutePrims primitives, one lane
+// per path: generate_path, then per bounce the closest hit (walk_all),
+// shade_path, and at once the NEE shadow ray (walk_all, any hit). The path's
+// radiance receives the same additions in the same order as through the
+// wavefront kernels (bounce b's emission, then its shadow contribution, then
+// bounce b+1's emission), so the sums are bit for bit those of
+// k_generate/k_trace/k_shade, and the path's total goes to radiance[p] for
+// k_accumulate. The scene is read from L1; no path state leaves the SM.
+// Lanes whose paths end take new ones from a work counter (a.counts[0])
+// once kPathRefill lanes of the warp are idle.
+constexpr uint32_t kPathRefill = 8;
+
+__global__ void __launch_bounds__(kBlock, 8) k_paths(WaveArgs a) {
+  const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
+  const ctk::SceneDev& sc = a.scene;
+  uint32_t fallbacks = 0;
+  float4 qa = make_float4(0, 0, 0, 0), qb = qa, qc = qa;
+  float lr = 0.0f, lg = 0.0f, lb = 0.0f;
+  int32_t bounce = -1;  // < 0: no path
+  uint32_t p = 0;
+  bool drained = false;
+  for (;;) {
+    const bool idle = bounce < 0;
+    const uint32_t want = __ballot_sync(0xffffffffu, idle);
+    if (!drained && (__popc(want) >= kPathRefill || want == 0xffffffffu)) {
+      const uint32_t leader = __ffs(want) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(a.counts, (uint32_t)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + __popc(want) >= a.paths) drained = true;
+      if (idle) {
+        const uint32_t k = base + __popc(want & lt_mask);
+        if (k < a.paths) {
+          p = k;
+          const uint32_t pass = p / a.pixels;
+          generate_path(a.frame, a.width, a.height, p - pass * a.pixels, a.first_frame + pass, p, qa, qb, qc);
+          lr = lg = lb = 0.0f;
+          bounce = 0;
+        }
+      }
+    }
+    if (drained && __all_sync(0xffffffffu, bounce < 0)) break;
+    if (bounce < 0) continue;
+    ctk::RayF r{qa.x, qa.y, qa.z, qb.x, qb.y, qb.z, ctk::kTMin, INFINITY, 0.0f, 0.0f, 0.0f};
+    ctk::finish_ray(r);
+    ctk::HitF h{-1, r.tmax, 0.0f, 0.0f, 0.0f};
+    ctk::walk_all<false>(sc, r, h, false, fallbacks);
+    ShadeOut so;
+    shade_path(sc, a.sky, 0, qa, qb, qc, h.prim, h.t, bounce, a.max_bounces, a.rr, a.nee, so);
+    if (so.lr != 0.0f || so.lg != 0.0f || so.lb != 0.0f) lr += so.lr, lg += so.lg, lb += so.lb;
+    if (so.shadow) {
+      ctk::RayF sr{so.sa.x, so.sa.y, so.sa.z, so.sb.x, so.sb.y, so.sb.z, ctk::kTMin, so.sa.w, 0.0f, 0.0f, 0.0f};
+      ctk::finish_ray(sr);
+      ctk::HitF sh{-1, sr.tmax, 0.0f, 0.0f, 0.0f};
+      ctk::walk_all<false>(sc, sr, sh, true, fallbacks);
+      if (sh.prim < 0) lr += so.scol.x, lg += so.scol.y, lb += so.scol.z;
+    }
+    if (so.cont) {
+      qa = so.na, qb = so.nb, qc = so.nc;
+      bounce++;
+    } else {
+      a.radiance[p] = make_float4(lr, lg, lb, 0.0f);
+      bounce = -1;
     }
   }
 }
@@ -500,7 +608,7 @@ int persistent_grid(K kernel) {
 
 template <bool BATCH>
 struct Grids {
-  int gen = 0, trace[4] = {0, 0, 0, 0}, shade = 0, acc = 0;
+  int gen = 0, trace[4] = {0, 0, 0, 0}, shade = 0, acc = 0, paths = 0;
 };
 
 template <bool BATCH>
@@ -513,6 +621,7 @@ const Grids<BATCH>& grids() {
     r.trace[kWalkSkip] = persistent_grid(k_trace<kWalkSkip, BATCH>);
     r.shade = persistent_grid(k_shade<BATCH>);
     r.acc = BATCH ? persistent_grid(k_accumulate_batch) : persistent_grid(k_accumulate);
+    if (!BATCH) r.paths = persistent_grid(k_paths);
     return r;
   }();
   return g;

@@ -58,7 +58,7 @@ def test_batch_equals_single_renders(scenes, wave_paths, walk):
         for job, img in zip(jobs, imgs):
             want = _single(job, opts, info["walk"])
             assert np.isfinite(img).all()
-            assert np.allclose(img, want, rtol=1e-5, atol=1e-6), job.scene.packed.prim_count
+            assert np.array_equal(img, want), job.scene.packed.prim_count
         # a second run of the same graph adds the same passes again
         br.run()
         for img, again in zip(imgs, br.images()):
@@ -100,3 +100,22 @@ def test_batch_rejects_bad_jobs(scenes):
     with pytest.raises(ct.CausticError, match="wave_paths"):
         ct.BatchRenderer(jobs, opts, wave_paths=-1)
     jobs[0].scene.close()
+
+
+@pytest.mark.parametrize("scene_fn", [ct.cornell_unit_box, lambda: ct.CORNELL_BOX])
+def test_path_kernel_equals_wavefront(native_lib, scene_fn):
+    """A scene of at most 32 primitives renders alone through the whole-path
+    kernel (k_paths) and in a batch through the wavefront kernels: the images
+    are equal bit for bit, with and without Russian roulette and NEE."""
+    scene = ct.DeviceScene.from_scene(scene_fn())
+    assert scene.walk == 2 and scene.packed.prim_count <= 32
+    frame = ct.camera_frame(scene_fn().camera, 40 / 30)
+    for rr, nee in [(False, True), (True, True), (True, False)]:
+        opts = ct.TraceOptions(max_bounces=8, russian_roulette=rr, nee=nee)
+        alone = ct.render_image(scene, frame, ct.RenderOptions(max_bounces=8, russian_roulette=rr, nee=nee,
+                                                               width=40, height=30, spp=9, seed=5))
+        with ct.BatchRenderer([ct.Job(scene, frame, 40, 30, 9, seed=5)], opts) as br:
+            br.run()
+            batch = br.images()[0]
+        assert np.array_equal(alone.reshape(-1), batch.reshape(-1)), (rr, nee)
+    scene.close()

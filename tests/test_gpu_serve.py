@@ -51,7 +51,7 @@ def test_each_request_same_alone_and_in_the_mix(device_scenes):
             max_bounces=OPTS.max_bounces, russian_roulette=OPTS.russian_roulette, nee=OPTS.nee,
             width=r.width, height=r.height, spp=r.spp, seed=r.seed))
         assert np.isfinite(want).all()
-        assert np.allclose(mixed[r.rid].reshape(want.shape), want, rtol=1e-5, atol=1e-6), r
+        assert np.array_equal(mixed[r.rid].reshape(want.shape), want), r
 
 
 def test_budget_limited_admission(device_scenes):
