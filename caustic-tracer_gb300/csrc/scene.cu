@@ -388,6 +388,10 @@ void destroy(ct_scene* s) {
     b->ptr = nullptr, b->bytes = 0;  // slices of the arena
   if (s->arena) path_free(s->arena, s->stream);
   s->io.release(&s->device_bytes);
+  for (cudaStream_t c : {s->copy_in, s->copy_out})
+    if (c) cudaStreamSynchronize(c), cudaStreamDestroy(c);
+  for (cudaEvent_t e : {s->ev_in, s->ev_done})
+    if (e) cudaEventDestroy(e);
   bool kept = false;
   if (s->stream && s->ev0 && s->ev1 && s->ev2 && s->device >= 0 && s->device < kPoolDevices &&
       cudaStreamSynchronize(s->stream) == cudaSuccess) {

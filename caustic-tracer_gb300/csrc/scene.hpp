@@ -74,6 +74,11 @@ struct ct_scene {
   int64_t opt_wave_paths = 0;
 
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+  // Copy streams and events of chunked host-pointer queries (created on the
+  // first such query): rays in on copy_in, results out on copy_out, while
+  // `stream` traces the chunk before.
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_done = nullptr;
 };
 
 namespace ct {

@@ -184,6 +184,10 @@ ct_status launch(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, floa
   return CT_OK;
 }
 
+// Rays per chunk of a pipelined host-pointer query (batches of at least two
+// chunks are pipelined).
+constexpr uint32_t kHostChunk = 1u << 22;
+
 // Host-pointer query: stage the rays, run, copy the results back.
 template <bool ANY>
 ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, float* t, float* u,
@@ -215,24 +219,58 @@ ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, 
     if (v) d_v = reinterpret_cast<float*>(o) + (next++) * (size_t)n;
   }
   cudaStream_t stream = s->stream;
+  // Large batches run in chunks: chunk k+1's rays go in on copy_in and chunk
+  // k-1's results come out on copy_out while chunk k is traced, so the
+  // copies hide behind the kernels (events order each chunk's copy in,
+  // trace and copy out). A small batch is one chunk on the scene stream.
+  const uint32_t chunks = n >= 2 * kHostChunk ? (n + kHostChunk - 1) / kHostChunk : 1;
+  cudaStream_t in = stream, out = stream;
+  if (chunks > 1) {
+    if (!s->copy_in) {
+      for (cudaStream_t* c : {&s->copy_in, &s->copy_out})
+        CT_CUDA(cudaStreamCreateWithFlags(c, cudaStreamNonBlocking));
+      for (cudaEvent_t* e : {&s->ev_in, &s->ev_done})
+        CT_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    in = s->copy_in;
+    out = s->copy_out;
+  }
   CT_CUDA(cudaMemsetAsync(s->counters.ptr, 0, 2 * sizeof(uint32_t), stream));
   CT_CUDA(cudaEventRecord(s->ev0, stream));
-  CT_CUDA(cudaMemcpyAsync(d_rays, rays, ray_bytes, cudaMemcpyHostToDevice, stream));
-  CT_CUDA(cudaEventRecord(s->ev1, stream));
-  st = launch<ANY>(s, d_rays, n, d_prim, d_t, d_u, d_v, d_blocked, stream);
-  if (st != CT_OK) return st;
-  CT_CUDA(cudaEventRecord(s->ev2, stream));
-  if (ANY) {
-    CT_CUDA(cudaMemcpyAsync(blocked, d_blocked, n, cudaMemcpyDeviceToHost, stream));
-  } else {
-    CT_CUDA(cudaMemcpyAsync(prim, d_prim, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
-    CT_CUDA(cudaMemcpyAsync(t, d_t, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
-    if (u) CT_CUDA(cudaMemcpyAsync(u, d_u, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
-    if (v) CT_CUDA(cudaMemcpyAsync(v, d_v, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+  if (chunks > 1) CT_CUDA(cudaStreamWaitEvent(in, s->ev0, 0));
+  for (uint32_t k = 0; k < chunks; k++) {
+    const size_t first = (size_t)k * kHostChunk;
+    const uint32_t m = chunks == 1 ? n : (uint32_t)std::min<size_t>(kHostChunk, n - first);
+    const size_t rf = first * CT_RAY_FLOATS;
+    CT_CUDA(cudaMemcpyAsync(d_rays + rf, rays + rf, (size_t)m * CT_RAY_FLOATS * sizeof(float),
+                            cudaMemcpyHostToDevice, in));
+    if (chunks > 1) {
+      CT_CUDA(cudaEventRecord(s->ev_in, in));
+      CT_CUDA(cudaStreamWaitEvent(stream, s->ev_in, 0));
+    }
+    if (k == 0) CT_CUDA(cudaEventRecord(s->ev1, stream));
+    st = launch<ANY>(s, d_rays + rf, m, ANY ? nullptr : d_prim + first, ANY ? nullptr : d_t + first,
+                     d_u ? d_u + first : nullptr, d_v ? d_v + first : nullptr, ANY ? d_blocked + first : nullptr,
+                     stream);
+    if (st != CT_OK) return st;
+    if (chunks > 1) {
+      CT_CUDA(cudaEventRecord(s->ev_done, stream));
+      CT_CUDA(cudaStreamWaitEvent(out, s->ev_done, 0));
+    }
+    if (ANY) {
+      CT_CUDA(cudaMemcpyAsync(blocked + first, d_blocked + first, m, cudaMemcpyDeviceToHost, out));
+    } else {
+      CT_CUDA(cudaMemcpyAsync(prim + first, d_prim + first, (size_t)m * 4, cudaMemcpyDeviceToHost, out));
+      CT_CUDA(cudaMemcpyAsync(t + first, d_t + first, (size_t)m * 4, cudaMemcpyDeviceToHost, out));
+      if (u) CT_CUDA(cudaMemcpyAsync(u + first, d_u + first, (size_t)m * 4, cudaMemcpyDeviceToHost, out));
+      if (v) CT_CUDA(cudaMemcpyAsync(v + first, d_v + first, (size_t)m * 4, cudaMemcpyDeviceToHost, out));
+    }
   }
+  CT_CUDA(cudaEventRecord(s->ev2, stream));
   uint32_t counters[2] = {0, 0};
-  CT_CUDA(cudaMemcpyAsync(counters, s->counters.ptr, sizeof counters, cudaMemcpyDeviceToHost, stream));
-  CT_CUDA(cudaStreamSynchronize(stream));
+  CT_CUDA(cudaMemcpyAsync(counters, s->counters.ptr, sizeof counters, cudaMemcpyDeviceToHost, out));
+  CT_CUDA(cudaStreamSynchronize(out));
+  if (chunks > 1) CT_CUDA(cudaStreamSynchronize(stream));
   if (counters[1]) return fail(CT_ERR_UNSUPPORTED, "traversal stack overflow (stack need %u)", s->stack_need);
   if (stats) {
     float k_ms = 0, all_ms = 0;
@@ -242,7 +280,7 @@ ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, 
     stats->total_ms = all_ms;
     stats->rays = n;
     stats->fp64_fallbacks = counters[0];
-    stats->launches = 1;
+    stats->launches = chunks;
   }
   return CT_OK;
 }

@@ -220,7 +220,11 @@ int32_t ct_scene_walk(const ct_scene* scene);
  * intersectClosest (intersect.ts:202-282) over a batch of rays. rays holds
  * CT_RAY_FLOATS floats per ray. prim receives the packed primitive index or
  * -1, t the hit distance (+inf on a miss); u, v (may be NULL) the triangle
- * barycentrics (0 for sphere hits). Host pointers.                          */
+ * barycentrics (0 for sphere hits). Host pointers. Batches of at least 8 Mi
+ * rays run in 4 Mi-ray chunks whose copies overlap the previous chunk's
+ * trace (pinned host memory lets the copies run asynchronously); stats then
+ * count one launch per chunk and kernel_ms spans the first chunk's trace to
+ * the last one's end.                                                      */
 ct_status ct_trace_closest(ct_scene* scene, const float* rays, uint32_t count, int32_t* prim,
                            float* t, float* u, float* v, ct_stats* stats);
 /* occluded (intersect.ts:368-420): blocked[i] = 1 when anything is hit in

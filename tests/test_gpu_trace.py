@@ -174,3 +174,34 @@ def test_reported_distance_bound_holds_on_grazing_and_far_geometry(oracle, nativ
         assert n_hit > 0.5 * len(rays)
         with_bary = ct.intersect_closest(dev, rays, barycentrics=True)  # the float64 refine path
         check_closest(oracle, packed, rays, with_bary, f"grazing@{offset}+uv")
+
+
+def test_pipelined_host_queries_equal_device_queries(native_lib):
+    """Host-pointer batches of more than two chunks (4 Mi rays each) are
+    copied in, traced and copied out in overlapping chunks; the answers equal
+    the device-pointer call's on the same rays, the ragged last chunk too."""
+    import ctypes as C
+
+    import torch
+    from caustic import _native
+
+    packed = ct.pack_scene(ct.triangle_soup(20_000, seed=9))
+    n = 2 * (1 << 22) + 12_345
+    rays = ct.soup_rays(n, seed=21)
+    with ct.DeviceScene(packed) as dev:
+        host = ct.intersect_closest(dev, rays, barycentrics=True)
+        assert host.stats.launches == 3
+        blocked = ct.occluded(dev, rays)
+        lib = _native.lib()
+        d_rays = torch.from_numpy(rays).cuda()
+        d_p = torch.empty(n, dtype=torch.int32, device="cuda")
+        d_t, d_u, d_v = (torch.empty(n, device="cuda") for _ in range(3))
+        _native.check(lib.ct_trace_closest_device(dev.handle, _native.ptr(d_rays), n, _native.ptr(d_p),
+                                                  _native.ptr(d_t), _native.ptr(d_u), _native.ptr(d_v), None))
+        d_b = torch.empty(n, dtype=torch.uint8, device="cuda")
+        _native.check(lib.ct_trace_occluded_device(dev.handle, _native.ptr(d_rays), n, _native.ptr(d_b), None))
+        torch.cuda.synchronize()
+        assert np.array_equal(host.prim, d_p.cpu().numpy())
+        for a, b in ((host.t, d_t), (host.u, d_u), (host.v, d_v)):
+            assert np.array_equal(a.view(np.uint32), b.cpu().numpy().view(np.uint32))
+        assert np.array_equal(blocked.astype(np.uint8), d_b.cpu().numpy())
