@@ -698,6 +698,8 @@ def run_batched(args, rank, world):
                                     "accumulatePass per frame (ct_accumulate_passes_device, passes = 1)"},
         "speedup_vs_per_frame": value / frame_rate,
         "clocks": clocks.summary(),
+        # kernel nodes of the graph (all nodes but one counter memset per wave), one replay per step
+        "gpu_launches": (info["graph_nodes"] - info["waves"]) * args.steps,
         "e2e": {"value": e2e_rate, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(sum(j.width * j.height * 12 for j in jobs)),
                 "what": "graph launch + device-to-host copy of all sums; scenes stay resident"},
