@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
     }
   };
   if (VARIANT == 0) {
-    ctk::walk_persistent<true, 8, false>(
+    ctk::walk_persistent<true, 6, false>(
         s, counters + kCountQueue, n,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);
