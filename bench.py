@@ -520,7 +520,8 @@ def roofline(args, prof, cpu, units_per_step, peak, peak_kind, scene_bytes=0):
            "compulsory_bytes_per_launch": comp, "compulsory_frac": rate(comp), "dram_frac": rate(traffic)}
     if args.workload == "cornell":
         out["note"] = ("14-primitive scene held in L1: the algorithmic bytes are re-read from L1, so frac > 1 "
-                       "is informational; dram_frac is the HBM traffic ncu measured per launch")
+                       "is informational; the kernel is bound by SM instruction issue, and dram_frac is the HBM "
+                       "traffic ncu measured per launch")
     return out
 
 
