@@ -39,11 +39,15 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   const uint64_t per_wave = std::max<uint64_t>(1, std::min<uint64_t>(passes, wave_paths / pixels));
   const uint64_t cap = per_wave * pixels;
   const int32_t B = o.max_bounces;
+  const int form = walk_form(s);
+  // Scenes of at most kBrutePrims primitives run whole paths per lane
+  // (k_paths): same sums as the wavefront kernels, no path queues.
+  const bool whole = form == kWalkSkip && s->prim_count <= ctk::kBrutePrims;
   // Path buffer: 2 queues + shadow queue (3 float4 each per path), radiance
-  // (float4), hit prim/t, counters.
+  // (float4), hit prim/t, counters; k_paths needs the radiance and counters.
   const size_t q_bytes = cap * sizeof(float4);
   const size_t counter_words = wave_counter_words(B);
-  const size_t bytes = 10 * q_bytes + cap * 8 + counter_words * 4 + 16 * 256;
+  const size_t bytes = (whole ? q_bytes : 10 * q_bytes + cap * 8) + counter_words * 4 + 16 * 256;
   void* buf = nullptr;
   ct_status st = path_alloc(s->device, bytes, stream, &buf);
   if (st != CT_OK) return st;
@@ -62,12 +66,14 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   a.scene = s->dev;
   a.sky = to_sky(s->sky);
   a.frame = to_frame(frame);
-  a.cur = Queue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes), nullptr};
-  a.next = Queue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes), nullptr};
-  a.shadow = ShadowQueue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes)};
+  if (!whole) {
+    a.cur = Queue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes), nullptr};
+    a.next = Queue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes), nullptr};
+    a.shadow = ShadowQueue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes)};
+    a.hit_prim = (int32_t*)take(cap * 4);
+    a.hit_t = (float*)take(cap * 4);
+  }
   a.radiance = (float4*)take(q_bytes);
-  a.hit_prim = (int32_t*)take(cap * 4);
-  a.hit_t = (float*)take(cap * 4);
   a.counts = (uint32_t*)take(counter_words * 4);
   a.width = width;
   a.height = height;
@@ -76,9 +82,7 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   a.rr = o.russian_roulette;
   a.nee = o.nee;
   const Grids<false>& g = grids<false>();
-  const int form = walk_form(s);
-  if (form == kWalkSkip && s->prim_count <= ctk::kBrutePrims) {
-    // Whole paths per lane (k_paths): same sums, no path queues.
+  if (whole) {
     for (uint64_t done = 0; done < passes; done += per_wave) {
       const uint32_t p = (uint32_t)std::min<uint64_t>(per_wave, passes - done);
       a.paths = (uint32_t)(p * pixels);
