@@ -196,7 +196,7 @@ ct_status ct_accumulate_pass(ct_scene* scene, const ct_camera_frame* frame, int3
   std::lock_guard<std::mutex> guard(scene->lock);
   CT_CUDA(cudaSetDevice(scene->device));
   const size_t n = (size_t)width * height * 3;
-  st = scene->io.reserve(n * sizeof(float), &scene->device_bytes);
+  st = scene->io.reserve(n * sizeof(float), &scene->device_bytes, scene->device, scene->stream);
   if (st != CT_OK) return st;
   cudaStream_t s = scene->stream;
   float* d = scene->io.as<float>();
@@ -227,7 +227,7 @@ ct_status ct_render_image(ct_scene* scene, const ct_camera_frame* frame, const c
   const size_t n = (size_t)o->width * o->height * 3;
   std::lock_guard<std::mutex> guard(scene->lock);
   CT_CUDA(cudaSetDevice(scene->device));
-  ct_status st = scene->io.reserve(n * sizeof(float), &scene->device_bytes);
+  ct_status st = scene->io.reserve(n * sizeof(float), &scene->device_bytes, scene->device, scene->stream);
   if (st != CT_OK) return st;
   float* d = scene->io.as<float>();
   CT_CUDA(cudaEventRecord(scene->ev0, scene->stream));

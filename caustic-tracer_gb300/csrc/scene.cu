@@ -21,30 +21,23 @@
 
 namespace ct {
 
-ct_status DeviceBuffer::reserve(size_t want, size_t* total_bytes) {
+ct_status DeviceBuffer::reserve(size_t want, size_t* total_bytes, int device, cudaStream_t stream) {
   if (want <= bytes) return CT_OK;
-  release(total_bytes);
+  release(total_bytes, stream);
   size_t grow = want + want / 4;
-  cudaError_t err = cudaMalloc(&ptr, grow);
-  if (err != cudaSuccess) {
-    ptr = nullptr;
-    (void)cudaGetLastError();
-    err = cudaMalloc(&ptr, want);
+  if (path_alloc(device, grow, stream, &ptr) != CT_OK) {
     grow = want;
-  }
-  if (err != cudaSuccess) {
-    ptr = nullptr;
-    (void)cudaGetLastError();
-    return fail(CT_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu bytes) failed: %s", want, cudaGetErrorString(err));
+    ct_status st = path_alloc(device, grow, stream, &ptr);
+    if (st != CT_OK) return st;
   }
   bytes = grow;
   if (total_bytes) *total_bytes += grow;
   return CT_OK;
 }
 
-void DeviceBuffer::release(size_t* total_bytes) {
+void DeviceBuffer::release(size_t* total_bytes, cudaStream_t stream) {
   if (ptr) {
-    cudaFree(ptr);
+    path_free(ptr, stream);
     if (total_bytes) *total_bytes -= bytes;
   }
   ptr = nullptr;
@@ -387,7 +380,7 @@ void destroy(ct_scene* s) {
                           &s->counters})
     b->ptr = nullptr, b->bytes = 0;  // slices of the arena
   if (s->arena) path_free(s->arena, s->stream);
-  s->io.release(&s->device_bytes);
+  s->io.release(&s->device_bytes, s->stream);
   for (cudaStream_t c : {s->copy_in, s->copy_out})
     if (c) cudaStreamSynchronize(c), cudaStreamDestroy(c);
   for (cudaEvent_t e : {s->ev_in, s->ev_done})

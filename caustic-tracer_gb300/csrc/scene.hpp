@@ -25,8 +25,10 @@ namespace ct {
 struct DeviceBuffer {
   void* ptr = nullptr;
   size_t bytes = 0;
-  ct_status reserve(size_t want, size_t* total_bytes);
-  void release(size_t* total_bytes);
+  // Grows to at least `want` bytes from the per-device pool (path_alloc), in
+  // the order of `stream`; release returns it there.
+  ct_status reserve(size_t want, size_t* total_bytes, int device, cudaStream_t stream);
+  void release(size_t* total_bytes, cudaStream_t stream);
   template <class T>
   T* as() const {
     return static_cast<T*>(ptr);

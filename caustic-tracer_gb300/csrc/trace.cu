@@ -201,7 +201,7 @@ ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, 
   if (n == 0) return CT_OK;
   const size_t ray_bytes = (size_t)n * CT_RAY_FLOATS * sizeof(float);
   const size_t out_words = ANY ? ((size_t)n + 3) / 4 : (size_t)n * (2 + (u ? 1 : 0) + (v ? 1 : 0));
-  ct_status st = s->io.reserve(ray_bytes + out_words * 4, &s->device_bytes);
+  ct_status st = s->io.reserve(ray_bytes + out_words * 4, &s->device_bytes, s->device, s->stream);
   if (st != CT_OK) return st;
   char* base = s->io.as<char>();
   float* d_rays = reinterpret_cast<float*>(base);
@@ -327,7 +327,7 @@ ct_status pick(ct_scene* s, const ct_camera_frame* frame, uint32_t n, const doub
   std::lock_guard<std::mutex> guard(s->lock);
   CT_CUDA(cudaSetDevice(s->device));
   const size_t ray_bytes = rays.size() * sizeof(float);
-  ct_status st = s->io.reserve(ray_bytes + (size_t)n * 12, &s->device_bytes);
+  ct_status st = s->io.reserve(ray_bytes + (size_t)n * 12, &s->device_bytes, s->device, s->stream);
   if (st != CT_OK) return st;
   char* base = s->io.as<char>();
   float* d_rays = reinterpret_cast<float*>(base);
