@@ -1,12 +1,15 @@
 """Autotuner for the integrator's launch choices.
 
 For a scene and a render size it times every admissible pair of
-(trace walk form, paths per wave) on a short render, applies the fastest to
-the scene (ct_scene_set_option) and records the measurements in a JSON table
-keyed by the scene's shape (primitive and node counts, tree depth) and the
-render size, so later renders of similar work reuse the choice without
+(trace walk form, paths per wave) on a short render, then, for the fastest
+pair, the launch shape of the trace kernels (resident 128-thread blocks per
+SM: as many as fit, or 8, 6 or 4), applies the fastest choice to the scene
+(ct_scene_set_option) and records the measurements in a JSON table keyed by
+the scene's shape (primitive and node counts, tree depth) and the render
+size, so later renders of similar work reuse the choice without
 re-measuring. Walk forms: 0 ordered walk per thread, 1 ordered walk with
-persistent lane refill, 2 stackless skip-link walk.
+persistent lane refill, 2 stackless skip-link walk. None of the choices
+changes an image, only the time it takes.
 """
 from __future__ import annotations
 
@@ -24,6 +27,8 @@ from .tracer import DeviceScene, RenderOptions
 
 OPT_WALK = 1
 OPT_WAVE_PATHS = 2
+OPT_TRACE_BLOCKS = 3
+BLOCK_CANDIDATES = (8, 6, 4)  # blocks per SM tried besides "as many as fit" (0)
 WALK_NAMES = {0: "ordered/thread", 1: "ordered/persistent", 2: "skip-link"}
 _lock = threading.Lock()
 
@@ -33,6 +38,7 @@ class Choice:
     walk: int
     wave_paths: int
     ms: float
+    blocks: int = 0  # trace blocks per SM (0: as many as fit)
 
 
 @dataclass
@@ -98,6 +104,10 @@ def autotune(dev: DeviceScene, frame: CameraFrame, opts: RenderOptions, table_pa
         apply(dev, Choice(walk, wave, 0.0))
         measured.append(Choice(walk, wave, _time_render(dev, frame, probe, reps)))
     best = min(measured, key=lambda c: c.ms)
+    for blocks in BLOCK_CANDIDATES:  # launch shape of the best pair
+        apply(dev, Choice(best.walk, best.wave_paths, 0.0, blocks))
+        measured.append(Choice(best.walk, best.wave_paths, _time_render(dev, frame, probe, reps), blocks))
+    best = min(measured, key=lambda c: c.ms)
     apply(dev, best)
     if table_path is not None:
         table[key] = {"best": asdict(best), "measured": [asdict(c) for c in measured]}
@@ -108,6 +118,7 @@ def autotune(dev: DeviceScene, frame: CameraFrame, opts: RenderOptions, table_pa
 def apply(dev: DeviceScene, choice: Choice) -> None:
     _native.check(dev._lib.ct_scene_set_option(dev.handle, OPT_WALK, int(choice.walk)))
     _native.check(dev._lib.ct_scene_set_option(dev.handle, OPT_WAVE_PATHS, int(choice.wave_paths)))
+    _native.check(dev._lib.ct_scene_set_option(dev.handle, OPT_TRACE_BLOCKS, int(choice.blocks)))
 
 
 def _load(path) -> Dict:

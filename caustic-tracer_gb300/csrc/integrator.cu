@@ -90,7 +90,7 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
       CT_CUDA(cudaMemsetAsync(a.counts, 0, counter_words * 4, stream));
       {
         ProfScope ps("paths", stream);
-        k_paths<<<g.paths, kBlock, 0, stream>>>(a);
+        k_paths<<<g.capped(g.paths, s->opt_trace_blocks), kBlock, 0, stream>>>(a);
       }
       {
         ProfScope ps("accumulate", stream);
@@ -102,7 +102,7 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   }
   auto trace = [&](const WaveArgs& w, int32_t b) {
     ProfScope ps("trace", stream);
-    launch_trace<false>(form, w, b, stream);
+    launch_trace<false>(form, w, b, stream, s->opt_trace_blocks);
   };
   for (uint64_t done = 0; done < passes; done += per_wave) {
     const uint32_t p = (uint32_t)std::min<uint64_t>(per_wave, passes - done);

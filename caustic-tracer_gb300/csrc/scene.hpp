@@ -71,9 +71,11 @@ struct ct_scene {
   size_t device_bytes = 0;
 
   // Tuning options (ct_scene_set_option): integrator walk form (-1 = chosen
-  // from the tree) and paths per wave (0 = library default).
+  // from the tree), paths per wave (0 = library default) and blocks per SM
+  // of the trace launches.
   int32_t opt_walk = -1;
   int64_t opt_wave_paths = 0;
+  int32_t opt_trace_blocks = 0;  // blocks per SM of trace launches (0 = occupancy)
 
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
   // Copy streams and events of chunked host-pointer queries (created on the

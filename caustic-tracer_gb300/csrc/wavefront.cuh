@@ -609,13 +609,19 @@ int persistent_grid(K kernel) {
 
 template <bool BATCH>
 struct Grids {
-  int gen = 0, trace[4] = {0, 0, 0, 0}, shade = 0, acc = 0, paths = 0;
+  int gen = 0, trace[4] = {0, 0, 0, 0}, shade = 0, acc = 0, paths = 0, sms = 1;
+  // `full` (the kernel's SMs x occupancy) capped at `blocks` per SM (0: uncapped).
+  int capped(int full, int blocks) const { return blocks > 0 ? std::min(full, sms * blocks) : full; }
 };
 
 template <bool BATCH>
 const Grids<BATCH>& grids() {
   static Grids<BATCH> g = [] {
     Grids<BATCH> r;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&r.sms, cudaDevAttrMultiProcessorCount, dev);
+    r.sms = std::max(1, r.sms);
     r.gen = persistent_grid(k_generate<BATCH>);
     r.trace[kWalkThread] = persistent_grid(k_trace<kWalkThread, BATCH>);
     r.trace[kWalkPersistent] = persistent_grid(k_trace<kWalkPersistent, BATCH>);
@@ -629,17 +635,18 @@ const Grids<BATCH>& grids() {
 }
 
 template <bool BATCH>
-void launch_trace(int form, const WaveArgs& w, int32_t bounce, cudaStream_t stream) {
+void launch_trace(int form, const WaveArgs& w, int32_t bounce, cudaStream_t stream, int blocks_per_sm = 0) {
   const Grids<BATCH>& g = grids<BATCH>();
   switch (form) {
     case kWalkPersistent:
-      k_trace<kWalkPersistent, BATCH><<<g.trace[kWalkPersistent], kBlock, 0, stream>>>(w, bounce);
+      k_trace<kWalkPersistent, BATCH><<<g.capped(g.trace[kWalkPersistent], blocks_per_sm), kBlock, 0, stream>>>(
+          w, bounce);
       break;
     default:
-      k_trace<kWalkThread, BATCH><<<g.trace[kWalkThread], kBlock, 0, stream>>>(w, bounce);
+      k_trace<kWalkThread, BATCH><<<g.capped(g.trace[kWalkThread], blocks_per_sm), kBlock, 0, stream>>>(w, bounce);
       break;
     case kWalkSkip:
-      k_trace<kWalkSkip, BATCH><<<g.trace[kWalkSkip], kBlock, 0, stream>>>(w, bounce);
+      k_trace<kWalkSkip, BATCH><<<g.capped(g.trace[kWalkSkip], blocks_per_sm), kBlock, 0, stream>>>(w, bounce);
       break;
   }
 }

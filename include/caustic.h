@@ -207,9 +207,14 @@ uint64_t ct_scene_device_bytes(const ct_scene* scene);
  *   CT_OPT_WALK        integrator trace walk: -1 chosen from the tree (default),
  *                      0 ordered walk per thread, 1 ordered walk with persistent
  *                      lane refill, 2 stackless skip-link walk (intersect.ts:290)
- *   CT_OPT_WAVE_PATHS  paths in flight per wave (0 = library default, 8 Mi)    */
+ *   CT_OPT_WAVE_PATHS  paths in flight per wave (0 = library default, 8 Mi)
+ *   CT_OPT_TRACE_BLOCKS  resident 128-thread blocks per SM of the integrator's
+ *                      trace (or whole-path) launches of a single-scene render,
+ *                      1..64, capped at the kernel's occupancy (0 = as many as
+ *                      fit, the default). Changes timing only, not images.   */
 #define CT_OPT_WALK 1
 #define CT_OPT_WAVE_PATHS 2
+#define CT_OPT_TRACE_BLOCKS 3
 ct_status ct_scene_set_option(ct_scene* scene, int32_t option, int64_t value);
 /* Trace walk the integrator uses for the scene (0, 1 or 2 as above: the
  * CT_OPT_WALK value, or the choice from the tree); -1 for a NULL scene. A
