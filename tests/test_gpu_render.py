@@ -79,11 +79,22 @@ def test_furnace_roulette(furnace):  # furnace.test.ts:65-81
     assert abs(img.mean() - 5) / 5 < 0.03
 
 
+def _lens_unit_box():
+    """The benchmark box seen through a thin lens (radius 0.04, focused on the
+    spheres): exercises the lens sample of the camera ray (camera.ts:62-72)."""
+    import dataclasses
+
+    sc = ct.cornell_unit_box()
+    return dataclasses.replace(sc, camera=ct.camera_at((0, 0.5, 1.6), (0, 0.5, 0), 32, 0.04, 1.55))
+
+
 @pytest.mark.parametrize("scene_name,w,h,spp,rr,bounces", [("cornell", 96, 64, 16, True, 8),
                                                             ("unit", 64, 64, 16, False, 8),
+                                                            ("lens", 64, 64, 16, False, 8),
                                                             ("caustic", 96, 54, 16, True, 12)])
 def test_three_sigma_agreement(oracle, native_lib, scene_name, w, h, spp, rr, bounces):
-    sc = {"cornell": ct.CORNELL_BOX, "unit": ct.cornell_unit_box()}.get(scene_name) or ct.caustic_scene(level=4)
+    sc = {"cornell": ct.CORNELL_BOX, "unit": ct.cornell_unit_box(), "lens": _lens_unit_box()}.get(scene_name) or \
+        ct.caustic_scene(level=4)
     packed = ct.pack_scene(sc)
     frame = ct.camera_frame(sc.camera, w / h)
     with ct.DeviceScene(packed) as dev:
