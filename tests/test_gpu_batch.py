@@ -108,12 +108,18 @@ def _lens_box():
     return dataclasses.replace(ct.cornell_unit_box(), camera=ct.camera_at((0, 0.5, 1.6), (0, 0.5, 0), 32, 0.04, 1.55))
 
 
-@pytest.mark.parametrize("scene_fn", [ct.cornell_unit_box, lambda: ct.CORNELL_BOX, _lens_box])
+def _sky_box():
+    import dataclasses
+
+    return dataclasses.replace(ct.cornell_unit_box(), sky=ct.SkyGradient((0.35, 0.55, 0.95), (1.0, 0.95, 0.85), 1.5))
+
+
+@pytest.mark.parametrize("scene_fn", [ct.cornell_unit_box, lambda: ct.CORNELL_BOX, _lens_box, _sky_box])
 def test_path_kernel_equals_wavefront(native_lib, scene_fn):
     """A scene of at most 32 primitives renders alone through the whole-path
     kernel (k_paths) and in a batch through the wavefront kernels: the images
     are equal bit for bit, with and without Russian roulette and NEE, through
-    a pinhole and a thin lens."""
+    a pinhole and a thin lens, under no sky and a gradient sky."""
     scene = ct.DeviceScene.from_scene(scene_fn())
     assert scene.walk == 2 and scene.packed.prim_count <= 32
     frame = ct.camera_frame(scene_fn().camera, 40 / 30)

@@ -88,13 +88,26 @@ def _lens_unit_box():
     return dataclasses.replace(sc, camera=ct.camera_at((0, 0.5, 1.6), (0, 0.5, 0), 32, 0.04, 1.55))
 
 
+def _with_sky(sc):
+    """The scene under the reference's gradient sky (tracer.ts:39-47, 211-216)."""
+    import dataclasses
+
+    return dataclasses.replace(sc, sky=ct.SkyGradient((0.35, 0.55, 0.95), (1.0, 0.95, 0.85), 1.5))
+
+
+SCENES = {"cornell": lambda: ct.CORNELL_BOX, "unit": ct.cornell_unit_box, "lens": _lens_unit_box,
+          "caustic": lambda: ct.caustic_scene(level=4), "unit_sky": lambda: _with_sky(ct.cornell_unit_box()),
+          "soup_sky": lambda: _with_sky(ct.batch_scene(5, 2_000, 4))}
+
+
 @pytest.mark.parametrize("scene_name,w,h,spp,rr,bounces", [("cornell", 96, 64, 16, True, 8),
                                                             ("unit", 64, 64, 16, False, 8),
                                                             ("lens", 64, 64, 16, False, 8),
-                                                            ("caustic", 96, 54, 16, True, 12)])
+                                                            ("caustic", 96, 54, 16, True, 12),
+                                                            ("unit_sky", 64, 64, 16, True, 8),
+                                                            ("soup_sky", 64, 48, 16, True, 6)])
 def test_three_sigma_agreement(oracle, native_lib, scene_name, w, h, spp, rr, bounces):
-    sc = {"cornell": ct.CORNELL_BOX, "unit": ct.cornell_unit_box(), "lens": _lens_unit_box()}.get(scene_name) or \
-        ct.caustic_scene(level=4)
+    sc = SCENES[scene_name]()
     packed = ct.pack_scene(sc)
     frame = ct.camera_frame(sc.camera, w / h)
     with ct.DeviceScene(packed) as dev:
