@@ -18,16 +18,19 @@ namespace ct {
 namespace {
 
 constexpr uint64_t kMaxWavePaths = 8ull << 20;  // paths in flight per wave
-constexpr uint32_t kPersistentDepth = 16;      // tree depth above which traces refill lanes
 constexpr uint32_t kSkipMaxNodes = 31;         // trees this small use the stackless skip-link walk
 
 // Walk form of a scene's trace launches: the scene's CT_OPT_WALK when set,
-// else by tree size and depth (the stackless walk for small trees and for
-// trees whose ordered walk could outgrow its stack).
+// else the stackless walk for small trees and for trees whose ordered walk
+// could outgrow its stack, and the persistent ordered walk for the rest. (The
+// per-thread ordered walk, kept for CT_OPT_WALK and the autotuner, was the
+// default for trees of depth <= 16 until the persistent walk took two steps
+// per refill round: on the batched workload the persistent walk everywhere
+// runs 819 against 800 Msamples/s.)
 int walk_form(const ct_scene* s) {
   if (s->opt_walk >= 0) return s->opt_walk;
   if (s->node_count <= kSkipMaxNodes || s->stack_need > ctk::kStackSize) return kWalkSkip;
-  return s->depth > kPersistentDepth ? kWalkPersistent : kWalkThread;
+  return kWalkPersistent;
 }
 
 // Runs `passes` passes starting at frame index `first` and adds them to the

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kBlock) k_generate(WaveArgs a) {
 // Walk forms of the trace kernel (chosen per scene by the host):
 //   kWalkThread     ordered walk, one per thread in a grid-stride loop;
 //   kWalkPersistent ordered walk, lanes refill from a work counter as their
-//                   walks finish (pays off for deep trees);
+//                   walks finish (the default above 31 nodes);
 //   kWalkSkip       the reference's stackless skip-link walk (no stack; all
 //                   lanes visit nodes in the same order; for small trees;
 //                   scenes of <= 32 primitives test every primitive in the
