@@ -660,7 +660,8 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
 // calls walk_begin; finish(i, w) consumes the answer. Lanes whose queries are
 // answered are refilled as soon as REFILL lanes of the warp are idle, so
 // lanes keep stepping instead of waiting for the warp's slowest ray (6 suits
-// the exact query walk, 0.7 % ahead of 8; 16 the integrator's: measured). Each round of the
+// the exact query walk, 0.7 % ahead of 8; 12 the integrator's, 1.7 % ahead
+// of 16 on the batched soups and 0.5 % behind it on the caustic scene). Each round of the
 // loop takes two steps per lane, which halves the refill bookkeeping (one
 // step per round ran 5 % slower on the 1M-triangle query walk, three or four
 // 20-35 % slower). With PHASED, the second step of a round moves either the

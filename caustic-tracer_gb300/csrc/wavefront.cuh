@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
   // walk reads the base pointers as often as the single-scene kernel reads
   // its kernel parameters.
   if constexpr (FORM == kWalkPersistent && !BATCH) {
-    ctk::walk_persistent<false, 16, true>(
+    ctk::walk_persistent<false, 12, true>(
         a.scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
         finish, fallbacks);
   } else if constexpr (FORM == kWalkPersistent) {
     ctk::SceneDev lane_scene = a.jobs[0].scene;
-    ctk::walk_persistent<false, 16, true>(
+    ctk::walk_persistent<false, 12, true>(
         lane_scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);
