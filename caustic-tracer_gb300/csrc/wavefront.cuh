@@ -383,7 +383,7 @@ __device__ __forceinline__ void shade_path(const ctk::SceneDev& sc, const SkyF& 
         const float cos_s = ctk::dot3(s, ls.dir);
         if (cos_s > 0.0f && ls.pdf > 0.0f) {
           const float pdf_b = cos_s * ctk::kInvPi;
-          const float k = (cos_s * ctk::kInvPi * ctk::power_heuristic(ls.pdf, pdf_b)) / ls.pdf;
+          const float k = __fdividef(cos_s * ctk::kInvPi * ctk::power_heuristic(ls.pdf, pdf_b), ls.pdf);
           out.shadow = true;
           out.sa = make_float4(p.x, p.y, p.z, ls.dist * ctk::kShadowShorten);
           out.sb = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, __uint_as_float(pid));
