@@ -381,7 +381,7 @@ void destroy(ct_scene* s) {
     b->ptr = nullptr, b->bytes = 0;  // slices of the arena
   if (s->arena) path_free(s->arena, s->stream);
   s->io.release(&s->device_bytes, s->stream);
-  for (cudaStream_t c : {s->copy_in, s->copy_out})
+  for (cudaStream_t c : {s->copy_in, s->copy_out, s->compute2})
     if (c) cudaStreamSynchronize(c), cudaStreamDestroy(c);
   for (cudaEvent_t e : {s->ev_in, s->ev_done})
     if (e) cudaEventDestroy(e);

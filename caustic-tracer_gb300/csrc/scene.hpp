@@ -78,10 +78,10 @@ struct ct_scene {
   int32_t opt_trace_blocks = 0;  // blocks per SM of trace launches (0 = occupancy)
 
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
-  // Copy streams and events of chunked host-pointer queries (created on the
-  // first such query): rays in on copy_in, results out on copy_out, while
-  // `stream` traces the chunk before.
-  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  // Streams and events of chunked host-pointer queries (created on the first
+  // such query): rays in on copy_in, results out on copy_out, while `stream`
+  // and compute2 trace alternate chunks.
+  cudaStream_t copy_in = nullptr, copy_out = nullptr, compute2 = nullptr;
   cudaEvent_t ev_in = nullptr, ev_done = nullptr;
 };
 

@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
                                                float* __restrict__ t_out, float* __restrict__ u_out,
                                                float* __restrict__ v_out,
                                                uint8_t* __restrict__ blocked,
-                                               uint32_t* __restrict__ counters) {
+                                               uint32_t* __restrict__ counters, uint32_t* __restrict__ queue) {
   uint32_t fallbacks = 0;
   bool overflow = false;
   auto load = [&](uint32_t i, ctk::RayF& r) {
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
   };
   if (VARIANT == 0) {
     ctk::walk_persistent<true, 6, false>(
-        s, counters + kCountQueue, n,
+        s, queue, n,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);
           ctk::walk_begin(s, w, ANY);
@@ -138,22 +138,26 @@ int grid_for(uint32_t n) {
   return (int)(need < full ? (need > 0 ? need : 1) : full);
 }
 
+// `slot` picks the persistent walk's work counter (two launches may run at
+// once on two streams, each with its own).
 template <bool ANY>
 ct_status launch(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, float* t, float* u,
-                 float* v, uint8_t* blocked, cudaStream_t stream) {
+                 float* v, uint8_t* blocked, cudaStream_t stream, int slot = 0) {
   if (n == 0) return CT_OK;
   // A tree whose walk could outgrow the ordered walk's stack uses the stackless walk.
   const int chosen = g_variant.load();
   const int variant = (chosen == 1 || s->stack_need > ctk::kStackSize) ? 1 : chosen;
   const float4* r4 = reinterpret_cast<const float4*>(rays);
   uint32_t* cnt = s->counters.as<uint32_t>();
-  CT_CUDA(cudaMemsetAsync(cnt + kCountQueue, 0, sizeof(uint32_t), stream));  // persistent work counter
+  uint32_t* queue = cnt + kCountQueue + slot;
+  CT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), stream));  // persistent work counter
   {
     ProfScope ps(ANY ? "occluded" : "closest", stream);
     auto go = [&](auto variant_c, auto bary_c) {
       constexpr int V = decltype(variant_c)::value;
       constexpr bool B = decltype(bary_c)::value;
-      k_trace<V, ANY, B><<<grid_for<V, ANY, B>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt);
+      k_trace<V, ANY, B><<<grid_for<V, ANY, B>(n), 128, 0, stream>>>(s->dev, r4, n, prim, t, u, v, blocked, cnt,
+                                                                   queue);
     };
     using B0 = std::integral_constant<bool, false>;
     using B1 = std::integral_constant<bool, true>;
@@ -222,12 +226,15 @@ ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, 
   // Large batches run in chunks: chunk k+1's rays go in on copy_in and chunk
   // k-1's results come out on copy_out while chunk k is traced, so the
   // copies hide behind the kernels (events order each chunk's copy in,
-  // trace and copy out). A small batch is one chunk on the scene stream.
+  // trace and copy out). Consecutive chunks alternate between two compute
+  // streams (each with its own work counter), so a chunk's blocks start on
+  // the SMs its predecessor's draining warps leave. A small batch is one
+  // chunk on the scene stream.
   const uint32_t chunks = n >= 2 * kHostChunk ? (n + kHostChunk - 1) / kHostChunk : 1;
   cudaStream_t in = stream, out = stream;
   if (chunks > 1) {
     if (!s->copy_in) {
-      for (cudaStream_t* c : {&s->copy_in, &s->copy_out})
+      for (cudaStream_t* c : {&s->copy_in, &s->copy_out, &s->compute2})
         CT_CUDA(cudaStreamCreateWithFlags(c, cudaStreamNonBlocking));
       for (cudaEvent_t* e : {&s->ev_in, &s->ev_done})
         CT_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
@@ -237,24 +244,28 @@ ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, 
   }
   CT_CUDA(cudaMemsetAsync(s->counters.ptr, 0, 2 * sizeof(uint32_t), stream));
   CT_CUDA(cudaEventRecord(s->ev0, stream));
-  if (chunks > 1) CT_CUDA(cudaStreamWaitEvent(in, s->ev0, 0));
+  if (chunks > 1) {
+    CT_CUDA(cudaStreamWaitEvent(in, s->ev0, 0));
+    CT_CUDA(cudaStreamWaitEvent(s->compute2, s->ev0, 0));
+  }
   for (uint32_t k = 0; k < chunks; k++) {
     const size_t first = (size_t)k * kHostChunk;
     const uint32_t m = chunks == 1 ? n : (uint32_t)std::min<size_t>(kHostChunk, n - first);
     const size_t rf = first * CT_RAY_FLOATS;
     CT_CUDA(cudaMemcpyAsync(d_rays + rf, rays + rf, (size_t)m * CT_RAY_FLOATS * sizeof(float),
                             cudaMemcpyHostToDevice, in));
+    cudaStream_t compute = (k & 1) ? s->compute2 : stream;
     if (chunks > 1) {
       CT_CUDA(cudaEventRecord(s->ev_in, in));
-      CT_CUDA(cudaStreamWaitEvent(stream, s->ev_in, 0));
+      CT_CUDA(cudaStreamWaitEvent(compute, s->ev_in, 0));
     }
     if (k == 0) CT_CUDA(cudaEventRecord(s->ev1, stream));
     st = launch<ANY>(s, d_rays + rf, m, ANY ? nullptr : d_prim + first, ANY ? nullptr : d_t + first,
                      d_u ? d_u + first : nullptr, d_v ? d_v + first : nullptr, ANY ? d_blocked + first : nullptr,
-                     stream);
+                     compute, (int)(k & 1));
     if (st != CT_OK) return st;
     if (chunks > 1) {
-      CT_CUDA(cudaEventRecord(s->ev_done, stream));
+      CT_CUDA(cudaEventRecord(s->ev_done, compute));
       CT_CUDA(cudaStreamWaitEvent(out, s->ev_done, 0));
     }
     if (ANY) {
@@ -266,11 +277,14 @@ ct_status host_query(ct_scene* s, const float* rays, uint32_t n, int32_t* prim, 
       if (v) CT_CUDA(cudaMemcpyAsync(v + first, d_v + first, (size_t)m * 4, cudaMemcpyDeviceToHost, out));
     }
   }
-  CT_CUDA(cudaEventRecord(s->ev2, stream));
+  CT_CUDA(cudaEventRecord(s->ev2, out));  // after every chunk's trace (out has waited for each)
   uint32_t counters[2] = {0, 0};
   CT_CUDA(cudaMemcpyAsync(counters, s->counters.ptr, sizeof counters, cudaMemcpyDeviceToHost, out));
   CT_CUDA(cudaStreamSynchronize(out));
-  if (chunks > 1) CT_CUDA(cudaStreamSynchronize(stream));
+  if (chunks > 1) {
+    CT_CUDA(cudaStreamSynchronize(stream));
+    CT_CUDA(cudaStreamSynchronize(s->compute2));
+  }
   if (counters[1]) return fail(CT_ERR_UNSUPPORTED, "traversal stack overflow (stack need %u)", s->stack_need);
   if (stats) {
     float k_ms = 0, all_ms = 0;
