@@ -51,6 +51,8 @@ RAY_BYTES, HIT_BYTES, BOX_BYTES, TRI_BYTES, SPHERE_BYTES = 32, 16, 32, 48, 32
 ACCUM_BYTES_PER_SAMPLE = 12
 
 
+CT_OPT_PATH_KERNEL = 4  # include/caustic.h
+
 def parse_args():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -422,7 +424,8 @@ def run_gpu(args, rank, world):
     with ClockSampler(torch.cuda.current_device()) as clocks:
         for k in range(args.steps):
             if args.workload != "traversal":
-                flush.fill_(k & 0xFF)  # L2 flush outside the timed events
+                with torch.cuda.stream(stream):  # L2 flush, ordered before the step's start event
+                    flush.fill_(k & 0xFF)
             starts[k].record(stream)
             step()
             ends[k].record(stream)
@@ -433,6 +436,28 @@ def run_gpu(args, rank, world):
     value = units_per_step * args.steps * world / total_s / 1e6
 
     prof = kernel_profile(lib, dev, step, stream, args)
+    wavefront = None
+    if args.workload != "traversal" and packed.prim_count <= 32:
+        # the same render through the wavefront kernels (the form every larger scene takes)
+        _native.check(lib.ct_scene_set_option(dev.handle, CT_OPT_PATH_KERNEL, 0))
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                step()
+        torch.cuda.synchronize()
+        nsteps = max(3, min(args.steps, 10))
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+        for k, (w0, w1) in enumerate(ev):
+            with torch.cuda.stream(stream):  # L2 flush before the start event, as in the timed steps
+                flush.fill_(k & 0xFF)
+            w0.record(stream)
+            step()
+            w1.record(stream)
+        torch.cuda.synchronize()
+        _native.check(lib.ct_scene_set_option(dev.handle, CT_OPT_PATH_KERNEL, 1))
+        wave_s = sum(w0.elapsed_time(w1) for w0, w1 in ev) / 1e3
+        wavefront = {"value": units_per_step * nsteps / wave_s / 1e6, "unit": metric,
+                     "what": "the same render through the wavefront kernels (generate, trace, shade over "
+                             "compacted queues) instead of the whole-path kernel; identical images"}
     if launches_per_step is None:
         launches_per_step = prof.get("launches_per_step")
 
@@ -450,6 +475,8 @@ def run_gpu(args, rank, world):
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
     line["roofline"] = roofline(args, prof, cpu, units_per_step, hbm_peak, peak_kind, dev.device_bytes)
 
+    if wavefront:
+        line["wavefront"] = wavefront
     if not args.no_e2e:
         line["e2e"] = e2e(args, ct, lib, packed, dev, rank, world, device)
     dev.close()

@@ -45,7 +45,7 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   const int form = walk_form(s);
   // Scenes of at most kBrutePrims primitives run whole paths per lane
   // (k_paths): same sums as the wavefront kernels, no path queues.
-  const bool whole = form == kWalkSkip && s->prim_count <= ctk::kBrutePrims;
+  const bool whole = s->opt_path_kernel && form == kWalkSkip && s->prim_count <= ctk::kBrutePrims;
   // Path buffer: 2 queues + shadow queue (3 float4 each per path), radiance
   // (float4), hit prim/t, counters; k_paths needs the radiance and counters.
   const size_t q_bytes = cap * sizeof(float4);

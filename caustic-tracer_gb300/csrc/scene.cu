@@ -557,6 +557,10 @@ ct_status ct_scene_set_option(ct_scene* scene, int32_t option, int64_t value) {
       CT_CHECK_ARG(value >= 0 && value <= 64, "CT_OPT_TRACE_BLOCKS %lld outside [0, 64]", (long long)value);
       scene->opt_trace_blocks = (int32_t)value;
       return CT_OK;
+    case CT_OPT_PATH_KERNEL:
+      CT_CHECK_ARG(value == 0 || value == 1, "CT_OPT_PATH_KERNEL %lld is not 0 or 1", (long long)value);
+      scene->opt_path_kernel = value != 0;
+      return CT_OK;
     default:
       return ct::fail(CT_ERR_INVALID_ARGUMENT, "unknown scene option %d", option);
   }

@@ -76,6 +76,7 @@ struct ct_scene {
   int32_t opt_walk = -1;
   int64_t opt_wave_paths = 0;
   int32_t opt_trace_blocks = 0;  // blocks per SM of trace launches (0 = occupancy)
+  bool opt_path_kernel = true;   // whole-path kernel for scenes of <= 32 primitives
 
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
   // Streams and events of chunked host-pointer queries (created on the first

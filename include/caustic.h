@@ -215,6 +215,11 @@ uint64_t ct_scene_device_bytes(const ct_scene* scene);
 #define CT_OPT_WALK 1
 #define CT_OPT_WAVE_PATHS 2
 #define CT_OPT_TRACE_BLOCKS 3
+/*   CT_OPT_PATH_KERNEL 1 (default): single-scene renders of scenes of at most
+ *                      32 primitives run each path whole in one lane; 0: they
+ *                      run the wavefront kernels like every other scene. The
+ *                      images are the same bit for bit.                      */
+#define CT_OPT_PATH_KERNEL 4
 ct_status ct_scene_set_option(ct_scene* scene, int32_t option, int64_t value);
 /* Trace walk the integrator uses for the scene (0, 1 or 2 as above: the
  * CT_OPT_WALK value, or the choice from the tree); -1 for a NULL scene. A

@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 import caustic as ct
+from caustic import _native
 
 pytestmark = pytest.mark.gpu
 
@@ -131,4 +132,10 @@ def test_path_kernel_equals_wavefront(native_lib, scene_fn):
             br.run()
             batch = br.images()[0]
         assert np.array_equal(alone.reshape(-1), batch.reshape(-1)), (rr, nee)
+        # the same scene alone with the whole-path kernel switched off (CT_OPT_PATH_KERNEL = 0)
+        _native.check(scene._lib.ct_scene_set_option(scene.handle, 4, 0))
+        wave = ct.render_image(scene, frame, ct.RenderOptions(max_bounces=8, russian_roulette=rr, nee=nee,
+                                                              width=40, height=30, spp=9, seed=5))
+        _native.check(scene._lib.ct_scene_set_option(scene.handle, 4, 1))
+        assert np.array_equal(alone.reshape(-1), wave.reshape(-1)), (rr, nee)
     scene.close()
