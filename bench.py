@@ -28,7 +28,6 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
-import math
 import os
 import pathlib
 import statistics

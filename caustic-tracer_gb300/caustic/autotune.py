@@ -19,7 +19,7 @@ import os
 import pathlib
 import threading
 from dataclasses import asdict, dataclass, field
-from typing import Dict, List, Optional, Sequence, Tuple
+from typing import Dict, List, Optional, Tuple
 
 from . import _abi, _native
 from .camera import CameraFrame

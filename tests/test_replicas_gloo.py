@@ -8,7 +8,6 @@ import socket
 import subprocess
 import sys
 
-import pytest
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
