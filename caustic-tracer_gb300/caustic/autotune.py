@@ -101,7 +101,10 @@ def autotune(dev: DeviceScene, frame: CameraFrame, opts: RenderOptions, table_pa
                           width=opts.width, height=opts.height, spp=min(opts.spp, probe_spp), seed=opts.seed)
     measured = []
     for walk, wave in candidates(dev, opts):
-        apply(dev, Choice(walk, wave, 0.0))
+        try:
+            apply(dev, Choice(walk, wave, 0.0))
+        except _native.CausticError:  # e.g. an ordered walk whose stack this tree could outgrow
+            continue
         measured.append(Choice(walk, wave, _time_render(dev, frame, probe, reps)))
     best = min(measured, key=lambda c: c.ms)
     for blocks in BLOCK_CANDIDATES:  # launch shape of the best pair
