@@ -493,12 +493,14 @@ __global__ void __launch_bounds__(kBlock, 10) k_shade(WaveArgs a, int32_t bounce
 // k_generate/k_trace/k_shade, and the path's total goes to radiance[p] for
 // k_accumulate. The scene is read from L1; no path state leaves the SM.
 // Lanes whose paths end take new ones from a work counter (a.counts[0])
-// once kPathRefill lanes of the warp are idle. 10 blocks of 128 per SM (48
-// registers) and refill at 4 idle lanes: 2,184 Msamples/s on the Cornell box
-// against 2,142 at 8 blocks (64 registers) and 8 lanes; 16 lanes 1,994.
+// once kPathRefill lanes of the warp are idle. 9 blocks of 128 per SM (56
+// registers) and refill at 4 idle lanes (Cornell box, measured): 8 blocks
+// (64 registers) 2,142 Msamples/s at 8 lanes; 10 blocks (48 registers,
+// spilling) 2,297 at 4 lanes, 9 blocks 2,318; 11 or 12 blocks 2,090;
+// refill at 16 lanes 1,994, at 1 or 2 lanes 2,256-2,260.
 constexpr uint32_t kPathRefill = 4;
 
-__global__ void __launch_bounds__(kBlock, 10) k_paths(WaveArgs a) {
+__global__ void __launch_bounds__(kBlock, 9) k_paths(WaveArgs a) {
   const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
   const ctk::SceneDev& sc = a.scene;
   uint32_t fallbacks = 0;
