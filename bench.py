@@ -13,6 +13,11 @@ Workloads
   served    a request trace through the continuous-batching server, against
             one plain renderImage per request (throughput all queued at
             once; p50/p99 latency under Poisson arrivals).
+  display   tonemapBuffer of a 3840 x 2160 sum buffer into RGBA8 on the
+            device (ct_tonemap_device). Metric: Mpixels/s.
+
+The default line (cornell) also carries the traversal and caustic workloads
+as sub-records, each with its own value, roofline, CPU baseline and e2e.
 
 `value` is device time with inputs resident in HBM (CUDA events on the
 launching stream, max over ranks); `e2e` is the same metric through the
@@ -46,6 +51,8 @@ import numpy as np  # noqa: E402
 CORNELL = dict(width=512, height=512, spp=16, max_bounces=8, russian_roulette=False, nee=True, seed=1)
 CAUSTIC = dict(width=1920, height=1080, spp=64, max_bounces=12, russian_roulette=True, nee=True, seed=1)
 TRAVERSAL = dict(triangles=1_000_000, rays=16_777_216, scene_seed=2024, ray_seed=77)
+DISPLAY = dict(width=3840, height=2160, samples=64, exposure_ev=0.0, mode="aces", seed=11)
+SIZE_OVERRIDE = None  # (width, height, spp) of a render workload, for profiling captures
 RAY_BYTES, HIT_BYTES, BOX_BYTES, TRI_BYTES, SPHERE_BYTES = 32, 16, 32, 48, 32
 ACCUM_BYTES_PER_SAMPLE = 12
 
@@ -58,7 +65,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["cornell", "traversal", "caustic", "batched", "served"], default="cornell")
+    ap.add_argument("--workload", choices=["cornell", "traversal", "caustic", "batched", "served", "display"], default="cornell")
     ap.add_argument("--jobs", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--requests", type=int, default=128, help="served: number of requests")
     ap.add_argument("--trace", choices=["c5", "preview"], default="c5",
@@ -66,8 +73,11 @@ def parse_args():
                          "1-8 spp)")
     ap.add_argument("--small", action="store_true", help="reduced sizes for profiling captures")
     ap.add_argument("--rays", type=int, default=0, help="traversal: trace only this many rays (profiling)")
+    ap.add_argument("--size", default="", help="cornell/caustic: WxHxSPP instead of the configuration's (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="cornell: leave out the traversal and caustic sub-records of the default line")
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="--impl reference: seconds of oracle work in the calibration run (a step is a quarter)")
     return ap.parse_args()
@@ -167,42 +177,115 @@ def barrier(world: int):
 
 
 # ---- workloads --------------------------------------------------------------------
-def traversal_inputs(rank: int, small: bool, rays: int = 0):
+_SCENES: dict = {}
+_RAYS: dict = {}
+
+
+class OracleStream:
+    """Scene generators draw from the oracle's restatement of Rng inside this
+    block, so a process that times the reference algorithm never loads the
+    CUDA library (the draws are the same numbers either way)."""
+
+    def __enter__(self):
+        import caustic.rng as rng
+        import oracle_lib as oracle
+
+        self.prev = rng.set_stream(oracle.rng_stream_state)
+        return self
+
+    def __exit__(self, *exc):
+        import caustic.rng as rng
+
+        rng.set_stream(self.prev)
+
+
+def _pack(scene, oracle_pack: bool):
+    """packScene through the library's packer, or the oracle's (the reference arm)."""
+    if oracle_pack:
+        import oracle_lib as oracle
+
+        return oracle.pack(scene)
+    import caustic as ct
+
+    return ct.pack_scene(scene)
+
+
+def traversal_inputs(rank: int, small: bool, rays: int = 0, oracle_pack: bool = False):
+    """The 1,000,000-triangle soup (packed) and the 16,777,216 query rays (cached per process)."""
+    import contextlib
+
     import caustic as ct
 
     tris = 100_000 if small else TRAVERSAL["triangles"]
     nrays = rays or ((1 << 20) if small else TRAVERSAL["rays"])
-    packed = ct.pack_scene(ct.triangle_soup(tris, seed=TRAVERSAL["scene_seed"]))
-    rays = ct.soup_rays(nrays, seed=TRAVERSAL["ray_seed"] + rank)
-    return packed, rays
+    ctx = OracleStream() if oracle_pack else contextlib.nullcontext()
+    key = ("traversal", small, oracle_pack)
+    with ctx:
+        if key not in _SCENES:
+            _SCENES[key] = _pack(ct.triangle_soup(tris, seed=TRAVERSAL["scene_seed"]), oracle_pack)
+        rkey = (rank, nrays)
+        if rkey not in _RAYS:
+            _RAYS[rkey] = ct.soup_rays(nrays, seed=TRAVERSAL["ray_seed"] + rank)
+    return _SCENES[key], _RAYS[rkey]
 
 
-def render_inputs(workload: str, small: bool):
-    """Packed scene, camera frame and render options of a render workload."""
-    import caustic as ct
-
+def render_cfg(workload: str, small: bool) -> dict:
+    if workload == "display":
+        cfg = dict(DISPLAY)
+        if small:
+            cfg.update(width=1920, height=1080)
+        return cfg
     if workload == "caustic":
         cfg = dict(CAUSTIC)
         if small:
             cfg.update(width=480, height=270, spp=4)
-        scene = ct.caustic_scene(level=5 if small else 7)
     else:
         cfg = dict(CORNELL)
         if small:
             cfg.update(width=128, height=128, spp=4)
-        scene = ct.cornell_unit_box()
-    packed = ct.pack_scene(scene)
-    frame = ct.camera_frame(scene.camera, cfg["width"] / cfg["height"])
+    if SIZE_OVERRIDE:
+        cfg.update(width=SIZE_OVERRIDE[0], height=SIZE_OVERRIDE[1], spp=SIZE_OVERRIDE[2])
+    return cfg
+
+
+def display_inputs(small: bool):
+    """A seeded synthetic sum buffer (width*height*3 float32) for the display
+    workload: per-channel radiance log-normal around 0.37 (sigma 1.5) times
+    the sample count, so both tone curves and their clamps are exercised."""
+    key = ("display", small)
+    if key not in _SCENES:
+        cfg = render_cfg("display", small)
+        rng = np.random.default_rng(cfg["seed"])
+        n = cfg["width"] * cfg["height"] * 3
+        _SCENES[key] = (rng.lognormal(-1.0, 1.5, n) * cfg["samples"]).astype(np.float32)
+    return _SCENES[key], render_cfg("display", small)
+
+
+def render_inputs(workload: str, small: bool, oracle_pack: bool = False):
+    """Packed scene, camera frame and render options of a render workload (cached per process)."""
+    import contextlib
+
+    import caustic as ct
+
+    cfg = render_cfg(workload, small)
+    key = (workload, small, oracle_pack)
+    if key not in _SCENES:
+        with OracleStream() if oracle_pack else contextlib.nullcontext():
+            scene = ct.caustic_scene(level=5 if small else 7) if workload == "caustic" else ct.cornell_unit_box()
+            _SCENES[key] = (_pack(scene, oracle_pack), ct.camera_frame(scene.camera, cfg["width"] / cfg["height"]))
+    packed, frame = _SCENES[key]
     return packed, frame, cfg
 
 
 def cpu_reference(workload: str, small: bool, target_s: float = 12.0):
-    """Times the oracle (the reference algorithm in C++) on a bounded sample; returns a dict."""
+    """Times the oracle (the reference algorithm in C++, scenes packed by the
+    oracle's own packScene) on a bounded sample; returns a dict."""
     import oracle_lib as oracle
+    from caustic import _abi
 
     threads = os.cpu_count() or 1
     if workload == "traversal":
-        packed, rays = traversal_inputs(0, small)
+        packed, rays = traversal_inputs(0, small, oracle_pack=True)
         n = 1 << 14
         while True:
             t0 = time.perf_counter()
@@ -216,8 +299,21 @@ def cpu_reference(workload: str, small: bool, target_s: float = 12.0):
                 "sample": f"first {n} of the {len(rays)} rays, ordered walk (intersectClosest), {threads} threads",
                 "bytes_per_unit": bpr, "counts_per_ray": {"aabb": cnt[0] / n, "tri": cnt[1] / n, "sphere": cnt[2] / n},
                 "seconds": dt}
-    packed, frame, cfg = render_inputs(workload, small)
-    from caustic import _abi
+    if workload == "display":
+        sums, cfg = display_inputs(small)
+        w, h = cfg["width"], cfg["height"]
+        rows = 16
+        while True:
+            t0 = time.perf_counter()
+            oracle.tonemap(sums[: w * rows * 3], w, rows, cfg["samples"], cfg["exposure_ev"])
+            dt = time.perf_counter() - t0
+            if dt >= target_s / 8 or rows >= h:
+                break
+            rows = min(h, int(rows * max(2.0, min(8.0, target_s / 8 / max(dt, 1e-3)))))
+        return {"value": w * rows / dt / 1e6, "unit": "Mpixels/s", "cores": 1, "kind": "port",
+                "sample": f"{w}x{rows} pixels of the {w}x{h} sum buffer, tonemapBuffer (ACES), 1 thread",
+                "seconds": dt, "bytes_per_unit": 16}
+    packed, frame, cfg = render_inputs(workload, small, oracle_pack=True)
 
     # Rows of the image at full spp until the sample takes long enough.
     w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
@@ -271,6 +367,8 @@ def kernel_bytes_per_step(kernel: str, cpu: dict, units_per_step: int):
     scenes of at most 32 primitives): the ray-query and shading bytes of the
     path together, plus its 16 B radiance written.
     """
+    if kernel == "tonemap":  # 12 B of sums read, 4 B of RGBA written per pixel
+        return 16 * units_per_step
     if "bytes_per_unit" in cpu:  # traversal workload: one closest-hit query per unit
         return cpu["bytes_per_unit"] * units_per_step if kernel == "closest" else None
     w = cpu["work_per_sample"]
@@ -291,19 +389,59 @@ def kernel_bytes_per_step(kernel: str, cpu: dict, units_per_step: int):
     return per * units_per_step
 
 
-def run_reference(args, rank, world):
-    """The reference algorithm on the host cores: W warm-up and K timed steps, each step
-    one bounded sample of the workload (sized by a calibration run to cpu_seconds / 4, 2 s by default)."""
-    if rank != 0:
-        return
+def workload_name(workload: str, small: bool) -> str:
+    if workload == "display":
+        c = render_cfg(workload, small)
+        return (f"display: tonemapBuffer (ACES, sRGB, RGBA8) of a {c['width']}x{c['height']} sum buffer "
+                f"({c['samples']} samples per pixel)")
+    if workload == "traversal":
+        return ("traversal: 1,000,000-triangle soup, 16,777,216 rays, closest hit" if not small
+                else "traversal (small): 100,000 triangles, 1,048,576 rays")
+    c = render_cfg(workload, small)
+    if workload == "caustic":
+        return (f"caustic scene (icosphere level {5 if small else 7} glass blob, 64 spheres, checker ground, "
+                f"sphere light) {c['width']}x{c['height']}, {c['spp']} spp, depth {c['max_bounces']}, NEE on, "
+                f"RR after bounce 3")
+    return f"cornell box {c['width']}x{c['height']}, {c['spp']} spp, depth {c['max_bounces']}, NEE on, RR off"
+
+
+def workload_config(workload: str, small: bool, gpus: int):
+    if workload == "traversal":
+        return {"workload": workload_name(workload, small),
+                "triangles": 100_000 if small else TRAVERSAL["triangles"],
+                "rays": (1 << 20) if small else TRAVERSAL["rays"],
+                "l2": "inputs larger than L2 (rays 512 MiB per step)", "parallelism": f"replicas x{gpus}"}
+    cfg = render_cfg(workload, small)
+    if SIZE_OVERRIDE and workload in ("cornell", "caustic"):
+        cfg["size_override"] = True
+    return {"workload": workload_name(workload, small), **cfg,
+            "l2": "L2 flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{gpus}"}
+
+
+def reference_record(workload: str, args, steps: int, warmup: int, cpu_seconds: float):
+    """The reference algorithm on the host cores for one workload: `warmup`
+    untimed and `steps` timed steps, each one bounded sample of the workload
+    (sized by a calibration run to cpu_seconds / 4)."""
     import oracle_lib as oracle
     from caustic import _abi
 
     threads = os.cpu_count() or 1
-    rec = cpu_reference(args.workload, args.small, target_s=args.cpu_seconds)
-    step_s = args.cpu_seconds / 4
-    if args.workload == "traversal":
-        packed, rays = traversal_inputs(0, args.small)
+    rec = cpu_reference(workload, args.small, target_s=cpu_seconds)
+    step_s = cpu_seconds / 4
+    if workload == "display":
+        sums, cfg = display_inputs(args.small)
+        w, h = cfg["width"], cfg["height"]
+        rows = max(1, min(h, int(rec["value"] * 1e6 * step_s / w)))
+        sample = sums[: w * rows * 3]
+        units = w * rows
+
+        def step():
+            oracle.tonemap(sample, w, rows, cfg["samples"], cfg["exposure_ev"])
+
+        desc = f"{w}x{rows} pixels of the {w}x{h} sum buffer per step, tonemapBuffer (ACES), 1 thread"
+        threads = 1
+    elif workload == "traversal":
+        packed, rays = traversal_inputs(0, args.small, oracle_pack=True)
         n = max(1 << 12, min(len(rays), int(rec["value"] * 1e6 * step_s)))
         sample = rays[:n]
         units = n
@@ -313,7 +451,7 @@ def run_reference(args, rank, world):
 
         desc = f"first {n} of the {len(rays)} rays per step, ordered walk (intersectClosest), {threads} threads"
     else:
-        packed, frame, cfg = render_inputs(args.workload, args.small)
+        packed, frame, cfg = render_inputs(workload, args.small, oracle_pack=True)
         w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
         rows = max(1, min(h, int(rec["value"] * 1e6 * step_s / (w * spp))))
         opts = _abi.ct_render_options(w, rows, spp, cfg["max_bounces"], int(cfg["russian_roulette"]),
@@ -325,62 +463,85 @@ def run_reference(args, rank, world):
             oracle.render_image(packed, fs, opts, nthreads=threads)
 
         desc = f"{w}x{rows} pixels x {spp} spp of the {w}x{h} render per step, {threads} threads"
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         step()
     dt = time.perf_counter() - t0
-    value = units * args.steps / dt / 1e6
-    metric = "Mrays/s" if args.workload == "traversal" else "Msamples/s"
-    rec = {"value": value, "unit": metric, "cores": threads, "kind": "port", "sample": desc}
-    line = {
+    value = units * steps / dt / 1e6
+    metric = {"traversal": "Mrays/s", "display": "Mpixels/s"}.get(workload, "Msamples/s")
+    base = {"value": value, "unit": metric, "cores": threads, "kind": "port",
+            "sample": desc + "; scenes packed and seeded by the oracle (no CUDA library loaded)"}
+    return {
         "impl": "reference", "metric": metric, "value": value, "unit": metric, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "steps": steps, "warmup": warmup, "ms_per_step": dt * 1e3 / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": workload_config(args),
-        "cpu_baseline": {k: rec[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "e2e": {"value": rec["value"], "unit": metric, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "data": "synthetic", "config": workload_config(workload, args.small, args.gpus),
+        "cpu_baseline": base,
+        "e2e": {"value": value, "unit": metric, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the reference algorithm (the oracle, all host threads)
+    on rank 0 only. The default line also carries the traversal and caustic
+    workloads as sub-records (5 timed steps, 1 warm-up each)."""
+    if rank != 0:
+        return
+    from caustic import _native
+
+    line = reference_record(args.workload, args, args.steps, args.warmup, args.cpu_seconds)
+    if default_line(args):
+        for sub in SUB_WORKLOADS:
+            rec = reference_record(sub, args, min(args.steps, 5), min(args.warmup, 1), args.cpu_seconds)
+            line[sub] = {k: rec[k] for k in SUB_KEYS if k in rec}
+    try:
+        mapped = "libcaustic_gb300" in pathlib.Path("/proc/self/maps").read_text()
+    except OSError:
+        mapped = None
+    line["product_library_loaded"] = bool(_native._lib is not None or mapped)
     print(json.dumps(line), flush=True)
 
 
-def workload_config(args):
-    if args.workload == "traversal":
-        return {"workload": "traversal: 1,000,000-triangle soup, 16,777,216 rays, closest hit" if not args.small
-                else "traversal (small): 100,000 triangles, 1,048,576 rays",
-                "triangles": 100_000 if args.small else TRAVERSAL["triangles"],
-                "rays": (1 << 20) if args.small else TRAVERSAL["rays"],
-                "l2": "inputs larger than L2 (rays 512 MiB per step)", "parallelism": f"replicas x{args.gpus}"}
-    if args.workload == "caustic":
-        c = dict(CAUSTIC)
-        if args.small:
-            c.update(width=480, height=270, spp=4)
-        name = (f"caustic scene (icosphere level {5 if args.small else 7} glass blob, 64 spheres, checker ground, "
-                f"sphere light) {c['width']}x{c['height']}, {c['spp']} spp, depth {c['max_bounces']}, NEE on, RR after bounce 3")
-    else:
-        c = dict(CORNELL)
-        if args.small:
-            c.update(width=128, height=128, spp=4)
-        name = f"cornell box {c['width']}x{c['height']}, {c['spp']} spp, depth {c['max_bounces']}, NEE on, RR off"
-    return {"workload": name, **c, "l2": "L2 flushed between timed steps (256 MiB write)",
-            "parallelism": f"replicas x{args.gpus}"}
+SUB_WORKLOADS = ("traversal", "caustic")
+SUB_KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "config", "clocks",
+            "gpu_launches", "cpu_baseline", "roofline", "e2e")
+
+
+def default_line(args) -> bool:
+    """The default run (the Cornell headline) also measures traversal and caustic."""
+    return args.workload == "cornell" and not args.small and not args.headline_only
 
 
 def run_gpu(args, rank, world):
     import torch
 
-    import caustic as ct
-    from caustic import _abi, _native
-
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    line = measure(args.workload, args, rank, world, args.steps, args.warmup, headline=True)
+    if default_line(args):
+        for sub in SUB_WORKLOADS:
+            rec = measure(sub, args, rank, world, args.steps, args.warmup, headline=False)
+            line[sub] = {k: rec[k] for k in SUB_KEYS if k in rec}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure(workload: str, args, rank: int, world: int, steps: int, warmup: int, headline: bool):
+    """One workload on this rank's GPU: device-timed steps with inputs
+    resident, per-kernel profile, roofline, CPU baseline and e2e."""
+    import torch
+
+    import caustic as ct
+    from caustic import _native
+
     device = torch.device("cuda", torch.cuda.current_device())
     lib = _native.lib()
     stream = torch.cuda.Stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
     hbm_peak, peak_kind = peaks()
 
-    if args.workload == "traversal":
+    if workload == "traversal":
         packed, rays_np = traversal_inputs(rank, args.small, args.rays)
         n = len(rays_np)
         dev = ct.DeviceScene(packed)
@@ -392,9 +553,23 @@ def run_gpu(args, rank, world):
             _native.check(lib.ct_trace_closest_device(dev.handle, _native.ptr(d_rays), n, _native.ptr(d_prim),
                                                       _native.ptr(d_t), None, None, C.c_void_p(stream.cuda_stream)))
 
-        units_per_step, metric, launches_per_step = n, "Mrays/s", 1
+        units_per_step, metric = n, "Mrays/s"
+    elif workload == "display":
+        sums, cfg = display_inputs(args.small)
+        w, h = cfg["width"], cfg["height"]
+        d_sums = torch.from_numpy(sums).to(device)
+        d_rgba = torch.empty(w * h * 4, dtype=torch.uint8, device=device)
+        packed, dev = None, None
+        mode = {"aces": 0, "reinhard": 1}[cfg["mode"]]
+
+        def step():
+            _native.check(lib.ct_tonemap_device(_native.ptr(d_sums), w, h, float(cfg["samples"]),
+                                                float(cfg["exposure_ev"]), mode, _native.ptr(d_rgba),
+                                                C.c_void_p(stream.cuda_stream)))
+
+        units_per_step, metric = w * h, "Mpixels/s"
     else:
-        packed, frame, cfg = render_inputs(args.workload, args.small)
+        packed, frame, cfg = render_inputs(workload, args.small)
         dev = ct.DeviceScene(packed)
         w, h = cfg["width"], cfg["height"]
         d_out = torch.empty(w * h * 3, dtype=torch.float32, device=device)
@@ -408,21 +583,19 @@ def run_gpu(args, rank, world):
                                                      C.c_void_p(stream.cuda_stream)))
 
         units_per_step, metric = w * h * cfg["spp"], "Msamples/s"
-        launches_per_step = None
 
     # warm-up
     with torch.cuda.stream(stream):
-        for _ in range(max(3, args.warmup)):
+        for _ in range(max(3, warmup)):
             step()
     torch.cuda.synchronize()
-    lib.ct_profile_reset() if hasattr(lib, "ct_profile_reset") else None
     barrier(world)
     torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     with ClockSampler(torch.cuda.current_device()) as clocks:
-        for k in range(args.steps):
-            if args.workload != "traversal":
+        for k in range(steps):
+            if workload != "traversal":
                 with torch.cuda.stream(stream):  # L2 flush, ordered before the step's start event
                     flush.fill_(k & 0xFF)
             starts[k].record(stream)
@@ -432,18 +605,18 @@ def run_gpu(args, rank, world):
     barrier(world)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_s = max_over_ranks(sum(step_ms) / 1e3, world, device)
-    value = units_per_step * args.steps * world / total_s / 1e6
+    value = units_per_step * steps * world / total_s / 1e6
 
-    prof = kernel_profile(lib, dev, step, stream, args)
+    prof = kernel_profile(lib, step, stream, steps)
     wavefront = None
-    if args.workload != "traversal" and packed.prim_count <= 32:
+    if headline and workload in ("cornell", "caustic") and packed.prim_count <= 32:
         # the same render through the wavefront kernels (the form every larger scene takes)
         _native.check(lib.ct_scene_set_option(dev.handle, CT_OPT_PATH_KERNEL, 0))
         with torch.cuda.stream(stream):
             for _ in range(3):
                 step()
         torch.cuda.synchronize()
-        nsteps = max(3, min(args.steps, 10))
+        nsteps = max(3, min(steps, 10))
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
         for k, (w0, w1) in enumerate(ev):
             with torch.cuda.stream(stream):  # L2 flush before the start event, as in the timed steps
@@ -457,33 +630,37 @@ def run_gpu(args, rank, world):
         wavefront = {"value": units_per_step * nsteps / wave_s / 1e6, "unit": metric,
                      "what": "the same render through the wavefront kernels (generate, trace, shade over "
                              "compacted queues) instead of the whole-path kernel; identical images"}
-    if launches_per_step is None:
-        launches_per_step = prof.get("launches_per_step")
-
+    launches_per_step = prof.get("launches_per_step") or 0
+    clk = clocks.summary()
     line = {
-        "metric": metric, "value": value, "unit": metric, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+        "metric": metric, "value": value, "unit": metric, "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": total_s * 1e3 / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, Rng of the reference)",
-        "config": workload_config(args), "clocks": clocks.summary(), "gpu_launches": (launches_per_step or 0) * args.steps,
+        "config": workload_config(workload, args.small, args.gpus), "clocks": clk,
+        "gpu_launches": launches_per_step * steps,
     }
 
     # CPU baseline (rank 0, N = 1): the oracle on a bounded sample; also yields the algorithmic bytes/unit.
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_reference(args.workload, args.small, target_s=12.0)
+        cpu = cpu_reference(workload, args.small, target_s=12.0)
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
-    line["roofline"] = roofline(args, prof, cpu, units_per_step, hbm_peak, peak_kind, dev.device_bytes)
+    sm_count = torch.cuda.get_device_properties(device).multi_processor_count
+    line["roofline"] = roofline(workload, args.small, prof, cpu, units_per_step, hbm_peak, peak_kind,
+                                dev.device_bytes if dev else 0, sm_count, clk.get("sm_mhz"))
 
     if wavefront:
         line["wavefront"] = wavefront
     if not args.no_e2e:
-        line["e2e"] = e2e(args, ct, lib, packed, dev, rank, world, device)
-    dev.close()
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+        line["e2e"] = e2e(workload, args, ct, lib, packed, dev, rank, world, device, steps)
+    if dev:
+        dev.close()
+    del flush
+    torch.cuda.empty_cache()
+    return line
 
 
-def kernel_profile(lib, dev, step, stream, args):
+def kernel_profile(lib, step, stream, steps):
     """Per-kernel device times over a few profiled steps (CUDA events around every launch)."""
     import torch
 
@@ -491,7 +668,7 @@ def kernel_profile(lib, dev, step, stream, args):
         return {}
     lib.ct_profile_enable(1)
     lib.ct_profile_reset()
-    nsteps = max(2, min(args.steps, 5))
+    nsteps = max(2, min(steps, 5))
     with torch.cuda.stream(stream):
         for _ in range(nsteps):
             step()
@@ -512,6 +689,8 @@ def compulsory_bytes_per_step(kernel: str, cpu: dict, units_per_step: int):
     radiance written. The scene once per launch is added by the caller."""
     if kernel == "paths":
         return units_per_step * 16
+    if kernel == "tonemap":
+        return units_per_step * 16
     if kernel not in ("trace", "closest"):
         return None
     if "bytes_per_unit" in cpu:
@@ -520,11 +699,19 @@ def compulsory_bytes_per_step(kernel: str, cpu: dict, units_per_step: int):
     return units_per_step * (w["closest_rays"] * (RAY_BYTES + HIT_BYTES) + w["shadow_rays"] * RAY_BYTES)
 
 
-def roofline(args, prof, cpu, units_per_step, peak, peak_kind, scene_bytes=0):
-    """achieved = the reference algorithm's bytes per launch of the dominant
-    kernel / its mean CUDA-event duration. Beside it: the compulsory bytes
+def roofline(workload, small, prof, cpu, units_per_step, peak, peak_kind, scene_bytes, sm_count, sm_mhz):
+    """Roofline of the dominant kernel.
+
+    HBM-bound kernels: achieved = the reference algorithm's bytes per launch /
+    the kernel's mean CUDA-event duration; beside it the compulsory bytes
     (rays, hits, scene once) and the DRAM bytes ncu measured per launch, each
-    also as a fraction of the peak over the same duration."""
+    also as a fraction of the peak over the same duration.
+
+    The whole-path kernel (k_paths) keeps its scene in L1 and its path state in
+    registers, so HBM does not bound it: its roofline is SM instruction issue,
+    achieved = warp instructions per launch (ncu) / the mean launch duration
+    against one warp instruction per cycle per scheduler (4 per SM) at the
+    sampled SM clock. Its HBM figures stay in the `hbm` sub-record."""
     kernels = prof.get("kernels", {})
     if not kernels:
         return None
@@ -535,31 +722,46 @@ def roofline(args, prof, cpu, units_per_step, peak, peak_kind, scene_bytes=0):
     algo = per_step / launches_per_step if per_step else None
     comp_step = compulsory_bytes_per_step(name, cpu, units_per_step) if cpu else None
     comp = comp_step / launches_per_step + scene_bytes if comp_step else None
-    rec = traffic_record(args.workload + ("_small" if args.small else ""))
-    traffic = rec.get("dram_bytes_per_launch") if rec and rec.get("scope") == name else None
+    rec = traffic_record(workload + ("_small" if small else ""))
+    rec = rec if rec and rec.get("scope") == name else None
+    traffic = rec.get("dram_bytes_per_launch") if rec else None
     achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
     rate = lambda b: b / (avg_ms / 1e3) / 1e9 / peak if b else None  # noqa: E731
-    out = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+    share = k["ms"] / sum(v["ms"] for v in kernels.values())
+    hbm = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
            "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_kind} hbm_gbs",
-           "traffic": traffic, "algorithmic_bytes_per_launch": algo, "avg_launch_ms": avg_ms,
-           "share": k["ms"] / sum(v["ms"] for v in kernels.values()),
+           "traffic": traffic, "algorithmic_bytes_per_launch": algo, "avg_launch_ms": avg_ms, "share": share,
            "compulsory_bytes_per_launch": comp, "compulsory_frac": rate(comp), "dram_frac": rate(traffic)}
-    if args.workload == "cornell":
-        out["note"] = ("14-primitive scene held in L1: the algorithmic bytes are re-read from L1, so frac > 1 "
-                       "is informational; the kernel is bound by SM instruction issue, and dram_frac is the HBM "
-                       "traffic ncu measured per launch")
-    return out
+    if name != "paths":
+        if rec:
+            hbm["traffic_source"] = rec.get("source")
+        return hbm
+    hbm["note"] = ("14-primitive scene held in L1: the algorithmic bytes are re-read from L1 (frac > 1), and "
+                   "dram_frac is the HBM traffic ncu measured per launch")
+    clock = float(sm_mhz or 2070.0)
+    inst = rec.get("warp_instructions_per_launch") if rec else None
+    issue_peak = sm_count * 4 * clock * 1e6 / 1e9
+    achieved_issue = inst / (avg_ms / 1e3) / 1e9 if inst else None
+    paths_per_launch = units_per_step / launches_per_step
+    return {"bound": "issue", "kernel": name, "achieved": achieved_issue, "peak": issue_peak,
+            "unit": "G warp instructions/s", "frac": achieved_issue / issue_peak if achieved_issue else None,
+            "peak_source": f"{sm_count} SMs x 4 schedulers x 1 warp instruction per cycle at {clock:.0f} MHz "
+                           f"(median sampled SM clock)",
+            "traffic": traffic, "avg_launch_ms": avg_ms, "share": share,
+            "warp_instructions_per_path": inst / paths_per_launch if inst else None,
+            "threads_per_warp_instruction": rec.get("threads_per_warp_instruction") if rec else None,
+            "instructions_source": rec.get("source") if rec else None, "hbm": hbm}
 
 
-def e2e(args, ct, lib, packed, dev, rank, world, device):
+def e2e(workload, args, ct, lib, packed, dev, rank, world, device, steps):
     """Same metric through the host-pointer C-ABI calls, copies included."""
     import torch
 
     from caustic import _abi, _native
 
-    steps = max(1, min(args.steps, 5))
-    if args.workload == "traversal":
-        _, rays_np = traversal_inputs(rank, args.small)
+    steps = max(1, min(steps, 5))
+    if workload == "traversal":
+        _, rays_np = traversal_inputs(rank, args.small, args.rays)
         n = len(rays_np)
         rays_pin = torch.from_numpy(rays_np).pin_memory()
         prim_pin = torch.empty(n, dtype=torch.int32).pin_memory()
@@ -577,8 +779,29 @@ def e2e(args, ct, lib, packed, dev, rank, world, device):
             parts["kernels_ms"] += stats.kernel_ms
 
         h2d, d2h, units, metric = n * 32, n * 8, n, "Mrays/s"
+    elif workload == "display":
+        sums, cfg = display_inputs(args.small)
+        w, h = cfg["width"], cfg["height"]
+        sums_pin = torch.from_numpy(sums).pin_memory()
+        rgba_pin = torch.empty(w * h * 4, dtype=torch.uint8).pin_memory()
+        d_sums = torch.empty(sums.size, dtype=torch.float32, device=device)
+        d_rgba = torch.empty(w * h * 4, dtype=torch.uint8, device=device)
+        stream = torch.cuda.current_stream()
+        parts = {"wall_ms": 0.0}
+
+        def call():
+            t0 = time.perf_counter()
+            d_sums.copy_(sums_pin, non_blocking=True)
+            _native.check(lib.ct_tonemap_device(_native.ptr(d_sums), w, h, float(cfg["samples"]),
+                                                float(cfg["exposure_ev"]), 0, _native.ptr(d_rgba),
+                                                C.c_void_p(stream.cuda_stream)))
+            rgba_pin.copy_(d_rgba, non_blocking=True)
+            stream.synchronize()
+            parts["wall_ms"] += (time.perf_counter() - t0) * 1e3
+
+        h2d, d2h, units, metric = sums.nbytes, w * h * 4, w * h, "Mpixels/s"
     else:
-        _, frame, cfg = render_inputs(args.workload, args.small)
+        _, frame, cfg = render_inputs(workload, args.small)
         w, h = cfg["width"], cfg["height"]
         out = torch.empty(w * h * 3, dtype=torch.float32).pin_memory()
         ropts = ct.RenderOptions(max_bounces=cfg["max_bounces"], russian_roulette=cfg["russian_roulette"],
@@ -880,7 +1103,10 @@ def run_served(args, rank, world):
 
 
 def main():
+    global SIZE_OVERRIDE
     args = parse_args()
+    if args.size:
+        SIZE_OVERRIDE = tuple(int(x) for x in args.size.lower().split("x"))
     rank, world, local = dist_env()
     if world > 1:
         import torch

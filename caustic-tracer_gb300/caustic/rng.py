@@ -2,7 +2,10 @@
 
 `Rng` is the scalar form for small scene generators; `Rng.draw(n)` produces
 long streams through the library's ct_rng_stream so generators of million-
-triangle scenes stay fast while consuming the identical sequence.
+triangle scenes stay fast while consuming the identical sequence. A process
+that must not load the CUDA library (a CPU-only tool timing another
+implementation on the same inputs) installs another generator of the same
+stream with `set_stream`.
 """
 from __future__ import annotations
 
@@ -11,6 +14,21 @@ import ctypes as C
 import numpy as np
 
 M32 = 0xFFFFFFFF
+
+# stream(state, out, kind, lo, hi) -> new state; None = the library's ct_rng_stream
+_stream = None
+
+
+def set_stream(fn):
+    """Installs the generator behind Rng.draw and returns the previous one.
+
+    fn(state, out, kind, lo, hi) fills the float64 array `out` with draws
+    continuing from the raw xorshift `state` (kind 0 next(), 1 nextU32(),
+    2 range(lo, hi)) and returns the state reached. None restores the
+    library's ct_rng_stream."""
+    global _stream
+    prev, _stream = _stream, fn
+    return prev
 
 
 def pcg_hash(x: int) -> int:
@@ -62,10 +80,13 @@ class Rng:
 
     def draw(self, n: int, kind: str = "next", lo: float = 0.0, hi: float = 1.0) -> np.ndarray:
         """n consecutive draws (kind 'next', 'u32' or 'range'), advancing this stream."""
-        from . import _native
-
         out = np.empty(int(n), np.float64)
         k = {"next": 0, "u32": 1, "range": 2}[kind]
+        if _stream is not None:
+            self.state = int(_stream(self.state, out, k, float(lo), float(hi)))
+            return out
+        from . import _native
+
         self.state = int(_native.lib().ct_rng_stream(self.state, 1, int(n), k, float(lo), float(hi),
                                                       out.ctypes.data_as(C.POINTER(C.c_double))))
         return out

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 
+#include "profile.hpp"
 #include "scene.hpp"
 
 namespace ct {
@@ -96,8 +97,9 @@ ct_status launch_tonemap(const float* accum, int32_t width, int32_t height, doub
   CT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const uint64_t need = (pixels + kBlock - 1) / kBlock;
   const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sms * 8));
-  k_tonemap<<<grid, kBlock, 0, static_cast<cudaStream_t>(stream)>>>(accum, (uint32_t)pixels, inv, (float)inv,
-                                                                     mode == 0, out, stride, header);
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ProfScope ps("tonemap", s);
+  k_tonemap<<<grid, kBlock, 0, s>>>(accum, (uint32_t)pixels, inv, (float)inv, mode == 0, out, stride, header);
   CT_CUDA(cudaGetLastError());
   return CT_OK;
 }

@@ -33,6 +33,12 @@ int walk_form(const ct_scene* s) {
   return kWalkPersistent;
 }
 
+// Scenes of at most kBrutePrims primitives run whole paths per lane
+// (k_paths): same sums as the wavefront kernels, no path queues.
+bool whole_paths(const ct_scene* s, int form) {
+  return s->opt_path_kernel && form == kWalkSkip && s->prim_count <= ctk::kBrutePrims;
+}
+
 // Runs `passes` passes starting at frame index `first` and adds them to the
 // device sums accum (and sumsq when non-NULL).
 ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, uint32_t height, uint32_t first,
@@ -43,9 +49,7 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   const uint64_t cap = per_wave * pixels;
   const int32_t B = o.max_bounces;
   const int form = walk_form(s);
-  // Scenes of at most kBrutePrims primitives run whole paths per lane
-  // (k_paths): same sums as the wavefront kernels, no path queues.
-  const bool whole = s->opt_path_kernel && form == kWalkSkip && s->prim_count <= ctk::kBrutePrims;
+  const bool whole = whole_paths(s, form);
   // Path buffer: 2 queues + shadow queue (3 float4 each per path), radiance
   // (float4), hit prim/t, counters; k_paths needs the radiance and counters.
   const size_t q_bytes = cap * sizeof(float4);
@@ -158,6 +162,7 @@ ct_status render_locked(ct_scene* scene, const ct_camera_frame* frame, const ct_
 }  // namespace
 
 int integrator_walk_form(const ct_scene* s) { return walk_form(s); }
+bool integrator_whole_paths(const ct_scene* s) { return whole_paths(s, walk_form(s)); }
 
 }  // namespace ct
 
@@ -253,11 +258,12 @@ ct_status ct_render_image(ct_scene* scene, const ct_camera_frame* frame, const c
 
 // ---- accumulatePass without allocation ------------------------------------------
 //
-// Some callers cannot allocate device memory at the time they render: code
-// that is recording a CUDA graph (cudaMalloc is not allowed while a stream is
-// being captured), real-time loops that forbid allocation per frame, and
-// plugin hosts that hand the library a fixed memory budget at load time and
-// own every later allocation. ct_accumulate_pass_noalloc serves them: its
+// Some callers cannot allocate device memory at the time they render:
+// real-time loops that forbid allocation per frame (an allocation can wait on
+// the device and miss the frame), plugin hosts that hand the library a fixed
+// memory budget at load time and own every later allocation, and deployments
+// that reserve all device memory up front. ct_accumulate_pass_noalloc serves
+// them: its
 // scratch (path queues, shadow queue, per-path radiance, hit records, queue
 // counters) lives in the file-scope array below, which every GPU that loads
 // this library holds until the process exits. The scene (created earlier
@@ -265,29 +271,64 @@ ct_status ct_render_image(ct_scene* scene, const ct_camera_frame* frame, const c
 namespace ct {
 namespace {
 
+constexpr size_t round256(size_t n) { return (n + 255) & ~size_t(255); }
 constexpr uint32_t kNoAllocMaxPixels = CT_NOALLOC_MAX_PIXELS;
-constexpr size_t kNoAllocPathBytes = 10 * sizeof(float4) + 2 * sizeof(uint32_t);  // per path slot
 constexpr size_t kNoAllocCounterWords = 4096;
-constexpr size_t kNoAllocScratchBytes =
-    (size_t)kNoAllocMaxPixels * kNoAllocPathBytes + kNoAllocCounterWords * 4 + 16 * 256;
+// Bytes the carve in ct_accumulate_pass_noalloc takes for `pixels` path
+// slots and `words` queue counters: 10 float4 arrays (two path queues and
+// the shadow queue of three float4 each, the radiance), the hit prims and
+// distances, the counters, each start rounded up to 256 bytes. It grows with
+// both arguments, so the array sized for the maxima holds every accepted call.
+constexpr size_t noalloc_layout_bytes(size_t pixels, size_t words) {
+  return 10 * round256(pixels * sizeof(float4)) + 2 * round256(pixels * 4) + round256(words * 4);
+}
+constexpr size_t kNoAllocScratchBytes = noalloc_layout_bytes(kNoAllocMaxPixels, kNoAllocCounterWords);
+static_assert(kNoAllocScratchBytes <= (size_t)44 << 20, "the static scratch stays within 44 MiB");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
+// cuCtxGetCurrent through the runtime's driver entry points (no link against
+// libcuda): the scratch address belongs to the context it was looked up in.
+using CtxGetCurrent = int (*)(void**);
+CtxGetCurrent ctx_get_current() {
+  static const CtxGetCurrent fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrent>(p);
+  }();
+  return fn;
+}
+
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kMaxDevices] = {};
+struct NoAllocSlot {
+  void* ptr = nullptr;
+  void* ctx = nullptr;
+};
+NoAllocSlot g_noalloc[kMaxDevices];
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the host symbol itself is only a stand-in for it).
+// Device address of the scratch array on the current device (the host
+// symbol itself is only a stand-in for it). Looked up on the first call on a
+// device, and again whenever that device's current context differs from the
+// one the address was taken in (after a cudaDeviceReset the array has a new
+// address in the new primary context).
 ct_status noalloc_scratch(int device, void** out) {
   CT_CHECK_ARG(device >= 0 && device < kMaxDevices, "device %d beyond %d", device, kMaxDevices);
+  void* ctx = nullptr;
+  CtxGetCurrent get = ctx_get_current();
+  if (get && get(&ctx) != 0) ctx = nullptr;
   std::lock_guard<std::mutex> guard(g_noalloc_mu);
-  if (!g_noalloc_ptr[device]) {
+  NoAllocSlot& slot = g_noalloc[device];
+  if (!slot.ptr || !ctx || slot.ctx != ctx) {
     void* p = nullptr;
     CT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_ptr[device] = p;
+    slot.ptr = p;
+    slot.ctx = ctx;
   }
-  *out = g_noalloc_ptr[device];
+  *out = slot.ptr;
   return CT_OK;
 }
 
@@ -321,7 +362,7 @@ ct_status ct_accumulate_pass_noalloc(ct_scene* scene, const ct_camera_frame* fra
   char* base = static_cast<char*>(scratch);
   auto take = [&](size_t n) {
     char* p = base;
-    base += (n + 255) & ~size_t(255);
+    base += round256(n);
     return p;
   };
   const size_t q = pixels * sizeof(float4);
@@ -336,7 +377,6 @@ ct_status ct_accumulate_pass_noalloc(ct_scene* scene, const ct_camera_frame* fra
   a.hit_prim = (int32_t*)take(pixels * 4);
   a.hit_t = (float*)take(pixels * 4);
   a.counts = (uint32_t*)take(counter_words * 4);
-  CT_CHECK_ARG((size_t)(base - static_cast<char*>(scratch)) <= kNoAllocScratchBytes, "static scratch layout overflow");
   a.width = (uint32_t)width;
   a.height = (uint32_t)height;
   a.pixels = (uint32_t)pixels;
@@ -349,14 +389,19 @@ ct_status ct_accumulate_pass_noalloc(ct_scene* scene, const ct_camera_frame* fra
   // The array keeps the previous call's contents: the counters must start at zero.
   CT_CUDA(cudaMemsetAsync(a.counts, 0, counter_words * 4, s));
   const Grids<false>& g = grids<false>();
-  const int form = integrator_walk_form(scene);
-  k_generate<false><<<g.gen, kBlock, 0, s>>>(a);
-  WaveArgs w = a;
-  for (int32_t b = 0; b <= B + 1; b++) {
-    launch_trace<false>(form, w, b, s);
-    if (b > B) break;
-    k_shade<false><<<g.shade, kBlock, 0, s>>>(w, b);
-    std::swap(w.cur, w.next);
+  if (integrator_whole_paths(scene)) {
+    // the kernels ct_accumulate_pass runs for this scene: whole paths per lane
+    k_paths<<<g.capped(g.paths, scene->opt_trace_blocks), kBlock, 0, s>>>(a);
+  } else {
+    const int form = integrator_walk_form(scene);
+    k_generate<false><<<g.gen, kBlock, 0, s>>>(a);
+    WaveArgs w = a;
+    for (int32_t b = 0; b <= B + 1; b++) {
+      launch_trace<false>(form, w, b, s, scene->opt_trace_blocks);
+      if (b > B) break;
+      k_shade<false><<<g.shade, kBlock, 0, s>>>(w, b);
+      std::swap(w.cur, w.next);
+    }
   }
   k_accumulate<<<g.acc, kBlock, 0, s>>>(a.radiance, a.pixels, 1, accum, nullptr);
   CT_CUDA(cudaGetLastError());

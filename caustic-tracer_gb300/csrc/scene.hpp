@@ -46,6 +46,8 @@ void path_free(void* p, cudaStream_t s);
 // Trace walk the single-scene integrator uses for `s` (0 ordered per thread,
 // 1 ordered persistent, 2 stackless skip-link); see integrator.cu.
 int integrator_walk_form(const ct_scene* s);
+// True when renders of this scene run whole paths per lane (k_paths).
+bool integrator_whole_paths(const ct_scene* s);
 
 }  // namespace ct
 

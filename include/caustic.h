@@ -315,19 +315,23 @@ void ct_batch_destroy(ct_batch* batch);
 
 /* ---- accumulatePass without allocation ------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device
- * memory when they render: code recording a CUDA graph (cudaMalloc is not
- * allowed while a stream is captured), real-time loops that forbid per-frame
- * allocation, and plugin hosts that own every allocation after load time.
- * Same work as ct_accumulate_pass (one sample per pixel, seeded by
- * Rng.fromPixel(pixel, frame_index), added into accum), but all scratch lives
- * in one static device array of the library, sized for CT_NOALLOC_MAX_PIXELS
- * pixels (about 42 MiB; every GPU that loads the library holds it until the
- * process exits). Larger images are rejected with CT_ERR_INVALID_ARGUMENT.
- * accum is a device array (width*height*3 floats); the scene comes from
- * ct_scene_create. The first call on a device looks the array up once for
- * that device; make that first call before any stream capture. All calls
- * share the one array, so calls that overlap on the GPU (on different
- * streams or different scenes) race: order them on one stream.           */
+ * memory when they render: real-time loops that forbid allocation per frame
+ * (an allocation can stall on the device and miss the frame), plugin hosts
+ * that hand the library a fixed memory budget at load time and own every
+ * later allocation, and deployments that must reserve all device memory up
+ * front. Same work as ct_accumulate_pass (one sample per pixel, seeded by
+ * Rng.fromPixel(pixel, frame_index), added into accum, through the same
+ * kernels and launch shapes the scene's options select), but all scratch
+ * lives in one static device array of the library, sized for
+ * CT_NOALLOC_MAX_PIXELS pixels (42 MiB; every GPU that loads the library
+ * holds it until the process exits). Larger images are rejected with
+ * CT_ERR_INVALID_ARGUMENT. accum is a device array (width*height*3 floats);
+ * the scene comes from ct_scene_create. The first call on a device (and the
+ * first after that device's context was reset) looks the array's address up
+ * for that device; make that first call before any stream capture. All calls
+ * share the one array and it keeps the last call's contents (each call clears
+ * the queue counters it needs), so calls that overlap on the GPU (on
+ * different streams or different scenes) race: order them on one stream.  */
 #define CT_NOALLOC_MAX_PIXELS (512u * 512u)
 ct_status ct_accumulate_pass_noalloc(ct_scene* scene, const ct_camera_frame* frame, int32_t width,
                                      int32_t height, uint32_t frame_index, const ct_trace_options* opts,

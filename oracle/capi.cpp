@@ -126,6 +126,14 @@ void or_rng_stream(uint32_t seed, uint32_t n, int32_t kind, double lo, double hi
     out[i] = kind == 0 ? r.next() : kind == 1 ? (double)r.next_u32() : r.range(lo, hi);
 }
 
+uint32_t or_rng_stream_state(uint32_t state, uint64_t n, int32_t kind, double lo, double hi, double* out) {
+  Rng r(0);
+  r.state = state;
+  for (uint64_t i = 0; i < n; i++)
+    out[i] = kind == 0 ? r.next() : kind == 1 ? (double)r.next_u32() : r.range(lo, hi);
+  return r.state;
+}
+
 or_packed* or_pack(const ct_object* objects, uint32_t count, const ct_sky* sky) {
   or_packed* h = new or_packed;
   h->p = pack_scene(scene_from(objects, count, sky));

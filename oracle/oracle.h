@@ -29,6 +29,8 @@ uint32_t or_pcg_hash(uint32_t x);
 uint32_t or_seed_for(uint32_t pixel, uint32_t frame);
 /* n draws of Rng(seed).next() (kind 0), nextU32() (kind 1) or range(lo,hi) (kind 2) */
 void or_rng_stream(uint32_t seed, uint32_t n, int32_t kind, double lo, double hi, double* out);
+/* The same draws continuing from a raw xorshift state; returns the state reached. */
+uint32_t or_rng_stream_state(uint32_t state, uint64_t n, int32_t kind, double lo, double hi, double* out);
 
 /* packScene (pack.ts:195-223) of a scene description or of the CORNELL_BOX preset. */
 or_packed* or_pack(const ct_object* objects, uint32_t count, const ct_sky* sky);

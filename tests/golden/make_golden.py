@@ -15,7 +15,9 @@ import sys
 
 
 def main() -> None:
-    ref = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/caustic-tracer")
+    ref = pathlib.Path(sys.argv[1])
     here = pathlib.Path(__file__).resolve().parent
     src = ref / "out" / "cornell.ppm"
     dst = here / "cornell.ppm"

@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
                 "or_pcg_hash": (C.c_uint32, [C.c_uint32]),
                 "or_seed_for": (C.c_uint32, [C.c_uint32, C.c_uint32]),
                 "or_rng_stream": (None, [C.c_uint32, C.c_uint32, C.c_int32, C.c_double, C.c_double, P]),
+                "or_rng_stream_state": (C.c_uint32, [C.c_uint32, C.c_uint64, C.c_int32, C.c_double, C.c_double, P]),
                 "or_pack": (P, [C.POINTER(_abi.ct_object), C.c_uint32, C.POINTER(_abi.ct_sky)]),
                 "or_pack_cornell": (P, [C.POINTER(or_camera_settings)]),
                 "or_packed_view": (None, [P, V, C.POINTER(C.POINTER(C.c_uint32))]),
@@ -178,6 +179,12 @@ def rng_stream(seed: int, n: int, kind: int = 0, lo: float = 0.0, hi: float = 1.
     out = np.empty(n, np.float64)
     lib().or_rng_stream(seed, n, kind, lo, hi, _p(out))
     return out
+
+
+def rng_stream_state(state: int, out: np.ndarray, kind: int = 0, lo: float = 0.0, hi: float = 1.0) -> int:
+    """Fills `out` (float64) with draws continuing from the raw xorshift `state`; returns the state reached.
+    Same contract as caustic.rng's stream generators (installable with caustic.rng.set_stream)."""
+    return int(lib().or_rng_stream_state(state, len(out), kind, lo, hi, _p(out)))
 
 
 def camera_frame(settings: or_camera_settings, aspect: float) -> _abi.ct_camera_frame:
