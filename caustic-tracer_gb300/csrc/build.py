@@ -1,4 +1,6 @@
-"""Builds libcaustic_gb300.so for sm_103a into caustic-tracer_gb300/_build/.
+"""Builds libcaustic_gb300.so for sm_103a into caustic-tracer_gb300/_build/,
+and beside it the Node-API addon caustic_addon.node (napi/caustic_addon.c),
+linked against the library with an $ORIGIN run path.
 
 Each translation unit is compiled by its own nvcc process (in parallel), then
 linked into one shared library. Host C++ is compiled with -ffp-contract=off so
@@ -20,6 +22,8 @@ HERE = pathlib.Path(__file__).resolve().parent
 PKG = HERE.parent
 OUT_DIR = PKG / "_build"
 LIB = OUT_DIR / "libcaustic_gb300.so"
+ADDON = OUT_DIR / "caustic_addon.node"
+NAPI = PKG / "napi"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 SOURCES = ["pack_host.cpp", "profile.cpp", "scene.cu", "trace.cu", "integrator.cu", "batch.cu", "display.cu"]
 HEADERS = ["common.hpp", "scene.hpp", "traverse.cuh", "integrator.cuh", "wavefront.cuh", "profile.hpp",
@@ -57,8 +61,35 @@ def stale() -> bool:
     return any(p.stat().st_mtime > built for p in deps)
 
 
+def addon_stale() -> bool:
+    if not ADDON.exists():
+        return True
+    built = ADDON.stat().st_mtime
+    deps = [LIB, NAPI / "caustic_addon.c", NAPI / "node_api_min.h", PKG.parent / "include" / "caustic.h"]
+    return any(p.stat().st_mtime > built for p in deps)
+
+
+def build_addon(force: bool = False) -> pathlib.Path:
+    """The Node-API addon: plain C (gcc), Node-API symbols left for Node to provide at load time."""
+    if not force and not addon_stale():
+        return ADDON
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler (gcc) found for the Node-API addon")
+    tmp = OUT_DIR / (ADDON.name + ".tmp")
+    cmd = [cc, "-std=c11", "-O2", "-fPIC", "-shared", "-Wall", "-Wextra", "-Werror", f"-I{NAPI}",
+           f"-I{PKG.parent / 'include'}", str(NAPI / "caustic_addon.c"), "-o", str(tmp), f"-L{OUT_DIR}",
+           "-lcaustic_gb300", "-Wl,-rpath,$ORIGIN", "-lm"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"compiling the Node-API addon failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, ADDON)
+    return ADDON
+
+
 def build(force: bool = False) -> pathlib.Path:
     if not force and not stale():
+        build_addon()
         return LIB
     OUT_DIR.mkdir(parents=True, exist_ok=True)
     objs = [OUT_DIR / (pathlib.Path(s).stem + ".o") for s in SOURCES]
@@ -70,6 +101,7 @@ def build(force: bool = False) -> pathlib.Path:
     if res.returncode != 0:
         raise RuntimeError(f"linking failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    build_addon(force=True)
     return LIB
 
 
