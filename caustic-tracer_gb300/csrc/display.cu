@@ -6,7 +6,12 @@
 // 3e-4. Only a channel whose y lies within 2e-3 of a rounding boundary
 // (k + 0.5), or is not a number, is recomputed in float64 in the reference's
 // operation order, so every byte is the one the reference's float64 code
-// stores. One thread per pixel: 12 bytes read, 4 (or 3) written.
+// stores. One thread per pixel: 12 bytes read, 4 (or 3) written. The float64
+// recomputations (about 0.4 % of channels) do not run where they arise: a
+// thread queues the channel in its block's shared memory and stores a
+// provisional byte, and the block later recomputes its queue with every lane
+// busy, so the slow float64 unit never runs with one lane of a warp active
+// while the other 31 wait.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -52,12 +57,19 @@ __device__ float srgb32(float x) {
   return x <= 0.0031308f ? 12.92f * x : __fmaf_rn(1.055f, powf(x, 1.0f / 2.4f), -0.055f);
 }
 
-__device__ __forceinline__ uint8_t channel(float a, double inv, float inv32, int aces) {
+// The float32 byte of a channel; false when y is within kRoundMargin of a
+// rounding boundary or not a number, where only the float64 path decides.
+__device__ __forceinline__ bool channel32(float a, float inv32, int aces, uint8_t& byte) {
   const float x = a * inv32;
   const float y = srgb32(aces ? aces32(x) : reinhard32(x)) * 255.0f;
   const float frac = y - floorf(y);
-  if (fabsf(frac - 0.5f) > kRoundMargin) return (uint8_t)(frac > 0.5f ? floorf(y) + 1.0f : floorf(y));
-  const double xd = (double)a * inv;  // near a boundary (or NaN): the reference's float64 path
+  byte = (uint8_t)(frac > 0.5f ? floorf(y) + 1.0f : floorf(y));
+  return fabsf(frac - 0.5f) > kRoundMargin;
+}
+
+// The reference's float64 path (tonemap.ts:41-62) for one channel.
+__device__ __noinline__ uint8_t channel64(float a, double inv, int aces) {
+  const double xd = (double)a * inv;
   return store_byte(srgb64(aces ? aces64(xd) : reinhard64(xd)) * 255.0);
 }
 
@@ -68,23 +80,59 @@ struct Header {
   uint32_t len;
 };
 
+constexpr uint32_t kQueue = 2048;  // float64 recomputations a block queues before it drains them
+
+// Recomputes the block's queued channels (indices into accum) in float64 and
+// stores their bytes over the provisional ones; every thread of the block calls it.
+__device__ __forceinline__ void drain(const float* __restrict__ accum, double inv, int aces, uint8_t* px_out,
+                                      uint32_t stride, const uint32_t* queue, uint32_t* count) {
+  __syncthreads();  // the provisional stores and the queue entries are visible to the block
+  const uint32_t n = *count;
+  for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+    const uint32_t ch = queue[k];
+    px_out[(size_t)(ch / 3) * stride + ch % 3] = channel64(accum[ch], inv, aces);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *count = 0;
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(kBlock) k_tonemap(const float* __restrict__ accum, uint32_t pixels, double inv,
                                                     float inv32, int aces, uint8_t* __restrict__ out,
                                                     uint32_t stride, Header header) {
+  __shared__ uint32_t queue[kQueue];
+  __shared__ uint32_t count;
+  if (threadIdx.x == 0) count = 0;
   if (blockIdx.x == 0 && threadIdx.x < header.len) out[threadIdx.x] = (uint8_t)header.bytes[threadIdx.x];
   uint8_t* px_out = out + header.len;
   const uint32_t grid = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += grid) {
-    const float r = accum[3 * (size_t)i], g = accum[3 * (size_t)i + 1], b = accum[3 * (size_t)i + 2];
-    const uint8_t br = channel(r, inv, inv32, aces), bg = channel(g, inv, inv32, aces),
-                  bb = channel(b, inv, inv32, aces);
-    if (stride == 4) {
-      reinterpret_cast<uchar4*>(px_out)[i] = make_uchar4(br, bg, bb, 255);
-    } else {
-      uint8_t* o = px_out + 3 * (size_t)i;
-      o[0] = br, o[1] = bg, o[2] = bb;
+  __syncthreads();
+  // Block-uniform trip count (the drains synchronise the block).
+  for (uint32_t base = blockIdx.x * blockDim.x; base < pixels; base += grid) {
+    const uint32_t i = base + threadIdx.x;
+    if (i < pixels) {
+      const float r = accum[3 * (size_t)i], g = accum[3 * (size_t)i + 1], b = accum[3 * (size_t)i + 2];
+      uint8_t br, bg, bb;
+      const bool okr = channel32(r, inv32, aces, br), okg = channel32(g, inv32, aces, bg),
+                 okb = channel32(b, inv32, aces, bb);
+      if (!(okr && okg && okb)) {
+        const uint32_t n = (uint32_t)!okr + (uint32_t)!okg + (uint32_t)!okb;
+        uint32_t k = atomicAdd(&count, n);
+        if (!okr) queue[k++] = 3 * i;
+        if (!okg) queue[k++] = 3 * i + 1;
+        if (!okb) queue[k] = 3 * i + 2;
+      }
+      if (stride == 4) {
+        reinterpret_cast<uchar4*>(px_out)[i] = make_uchar4(br, bg, bb, 255);
+      } else {
+        uint8_t* o = px_out + 3 * (size_t)i;
+        o[0] = br, o[1] = bg, o[2] = bb;
+      }
     }
+    __syncthreads();
+    if (count > kQueue - 3 * kBlock) drain(accum, inv, aces, px_out, stride, queue, &count);
   }
+  drain(accum, inv, aces, px_out, stride, queue, &count);
 }
 
 ct_status launch_tonemap(const float* accum, int32_t width, int32_t height, double samples, double exposure_ev,

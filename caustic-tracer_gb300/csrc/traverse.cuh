@@ -590,15 +590,29 @@ __device__ __forceinline__ void walk_enter(Walk& w, int32_t c) {
   }
 }
 
-// One step; w.ref == kWalkDone when the query is answered.
+// One step; w.ref == kWalkDone when the query is answered. A step of the
+// exact walk tests one primitive of a leaf; a step of the integrator's walk
+// (plain float32 tests, a third of the instructions) tests the whole leaf,
+// which pays one memory latency per leaf instead of one per primitive
+// (caustic scene: 1,067 -> 1,214 Msamples/s, identical images; the exact
+// walk with whole-leaf steps ran at 645 against 895 Mrays/s).
 template <bool EXACT>
 __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& fallbacks) {
   if (w.ref == kWalkLeaf) {
-    if (test_prim<EXACT>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
-      w.ref = kWalkDone;
-      return;
+    if constexpr (EXACT) {
+      if (test_prim<EXACT>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
+        w.ref = kWalkDone;
+        return;
+      }
+      if (++w.cur == w.end) w.ref = kWalkPop;
+    } else {
+      for (; w.cur < w.end; w.cur++)
+        if (test_prim<EXACT>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
+          w.ref = kWalkDone;
+          return;
+        }
+      w.ref = kWalkPop;
     }
-    if (++w.cur == w.end) w.ref = kWalkPop;
   } else if (w.ref >= 0 && w.ref != kWalkPop) {
     const uint4* q = s.quads + (size_t)w.ref * 4;
     const uint4 bx = __ldg(q), by = __ldg(q + 1), bz = __ldg(q + 2);
