@@ -53,6 +53,10 @@ CAUSTIC = dict(width=1920, height=1080, spp=64, max_bounces=12, russian_roulette
 TRAVERSAL = dict(triangles=1_000_000, rays=16_777_216, scene_seed=2024, ray_seed=77)
 DISPLAY = dict(width=3840, height=2160, samples=64, exposure_ev=0.0, mode="aces", seed=11)
 SIZE_OVERRIDE = None  # (width, height, spp) of a render workload, for profiling captures
+# Paths a render needs to fill the GPU through its bounces: 152 SMs x 1,536
+# resident lanes of the trace kernels = 233,472, times 4 for the tail of later
+# bounces, where paths have ended.
+FILL_PATHS = 1 << 20
 RAY_BYTES, HIT_BYTES, BOX_BYTES, TRI_BYTES, SPHERE_BYTES = 32, 16, 32, 48, 32
 ACCUM_BYTES_PER_SAMPLE = 12
 
@@ -919,6 +923,19 @@ def run_batched(args, rank, world):
         t_batch = timed(batched_step, args.steps)
     t_plain = timed(plain_step, max(1, args.steps // 2))
     plain_rate = samples * max(1, args.steps // 2) * world / t_plain / 1e6
+    # Ceiling of any batching: jobs of at least FILL_PATHS paths already fill
+    # the GPU alone, and batching cannot render their samples faster than
+    # their own renderImage does; so the speedup over the plain loop is at
+    # most t_plain / (the plain time of those jobs alone).
+    big = [k for k, j in enumerate(jobs) if j.width * j.height * spp >= FILL_PATHS]
+
+    def plain_big_step():
+        for k in big:
+            j = jobs[k]
+            _native.check(lib.ct_render_image_device(j.scene.handle, C.byref(fstructs[k]), C.byref(ropts[k]),
+                                                     _native.ptr(outs[k]), C.c_void_p(stream.cuda_stream)))
+
+    t_big = timed(plain_big_step, max(1, args.steps // 2)) if big else 0.0
     t_frame = timed(per_frame_step, 1)
     frame_rate = samples * world / t_frame / 1e6
     value = samples * args.steps * world / t_batch / 1e6
@@ -947,6 +964,11 @@ def run_batched(args, rank, world):
         "plain_sequential": {"value": plain_rate, "unit": "Msamples/s",
                              "what": "the same jobs as consecutive ct_render_image_device calls"},
         "speedup_vs_plain": value / plain_rate,
+        "ceiling_vs_plain": {"value": t_plain / t_big if t_big else None, "large_jobs": len(big),
+                             "large_job_samples": int(sum(jobs[k].width * jobs[k].height * spp for k in big)),
+                             "what": f"plain time of all jobs / plain time of the jobs of at least {FILL_PATHS} "
+                                     "paths, which fill the GPU alone: an upper bound of any batching's speedup "
+                                     "over the plain loop (it assumes the other jobs cost nothing)"},
         "plain_per_frame": {"value": frame_rate, "unit": "Msamples/s",
                             "what": "the same jobs one after another, each as a progressive loop of one "
                                     "accumulatePass per frame (ct_accumulate_passes_device, passes = 1)"},
@@ -1057,6 +1079,13 @@ def run_served(args, rank, world):
     t_plain = max_over_ranks(t_plain, world, device)
     value = samples * args.steps * world / t_dev / 1e6
     plain_rate = samples * world / t_plain / 1e6
+    # Ceiling of any batching (as in the batched workload): the requests of at
+    # least FILL_PATHS paths rendered alone by the plain loop.
+    big = [r for r in trace if r.pixels * r.spp >= FILL_PATHS]
+    t0 = time.perf_counter()
+    render_plain(dev, at(big, None), opts, t0=t0)
+    torch.cuda.synchronize()
+    t_big = max_over_ranks(time.perf_counter() - t0, world, device) if big else 0.0
     _, t_frame = per_frame()
     t_frame = max_over_ranks(t_frame, world, device)
     frame_rate = samples * world / t_frame / 1e6
@@ -1083,6 +1112,11 @@ def run_served(args, rank, world):
         "plain_sequential": {"value": plain_rate, "unit": "Msamples/s",
                              "what": "the same requests as consecutive ct_render_image_device calls, one at a time"},
         "speedup_vs_plain": value / plain_rate,
+        "ceiling_vs_plain": {"value": t_plain / t_big if t_big else None, "large_requests": len(big),
+                             "large_request_samples": int(sum(r.pixels * r.spp for r in big)),
+                             "what": f"plain time of all requests / plain time of the requests of at least "
+                                     f"{FILL_PATHS} paths, which fill the GPU alone: an upper bound of any "
+                                     "batching's speedup over the plain loop"},
         "plain_per_frame": {"value": frame_rate, "unit": "Msamples/s",
                             "what": "the same requests one at a time, each as a progressive loop of one "
                                     "accumulatePass per frame (ct_accumulate_passes_device, passes = 1)"},
