@@ -510,7 +510,7 @@ def run_reference(args, rank, world):
 
 SUB_WORKLOADS = ("traversal", "caustic")
 SUB_KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "config", "clocks",
-            "gpu_launches", "cpu_baseline", "roofline", "e2e")
+            "gpu_launches", "cpu_baseline", "roofline", "e2e", "stackless")
 
 
 def default_line(args) -> bool:
@@ -634,6 +634,24 @@ def measure(workload: str, args, rank: int, world: int, steps: int, warmup: int,
         wavefront = {"value": units_per_step * nsteps / wave_s / 1e6, "unit": metric,
                      "what": "the same render through the wavefront kernels (generate, trace, shade over "
                              "compacted queues) instead of the whole-path kernel; identical images"}
+    stackless = None
+    if workload == "traversal":
+        # the same rays through the reference's stackless skip-link walk (intersect.ts:290-365)
+        prev = lib.ct_set_traversal(1)
+        with torch.cuda.stream(stream):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        lib.ct_set_traversal(prev)
+        stackless = {"value": units_per_step * 3 / (e0.elapsed_time(e1) / 1e3) / 1e6, "unit": metric,
+                     "what": "the same rays through the reference's stackless skip-link walk over its binary "
+                             "node array (intersectClosestStackless) instead of the ordered walk over 4-wide "
+                             "records; identical hits"}
     launches_per_step = prof.get("launches_per_step") or 0
     clk = clocks.summary()
     line = {
@@ -655,6 +673,8 @@ def measure(workload: str, args, rank: int, world: int, steps: int, warmup: int,
 
     if wavefront:
         line["wavefront"] = wavefront
+    if stackless:
+        line["stackless"] = stackless
     if not args.no_e2e:
         line["e2e"] = e2e(workload, args, ct, lib, packed, dev, rank, world, device, steps)
     if dev:
@@ -923,10 +943,10 @@ def run_batched(args, rank, world):
         t_batch = timed(batched_step, args.steps)
     t_plain = timed(plain_step, max(1, args.steps // 2))
     plain_rate = samples * max(1, args.steps // 2) * world / t_plain / 1e6
-    # Ceiling of any batching: jobs of at least FILL_PATHS paths already fill
-    # the GPU alone, and batching cannot render their samples faster than
-    # their own renderImage does; so the speedup over the plain loop is at
-    # most t_plain / (the plain time of those jobs alone).
+    # The plain loop on the jobs of at least FILL_PATHS paths alone: they
+    # fill the GPU by themselves and hold most of the samples, so the gap
+    # between this rate and the batched rate is what batching gains on them
+    # (bounce tails and per-render launches), not on small jobs.
     big = [k for k, j in enumerate(jobs) if j.width * j.height * spp >= FILL_PATHS]
 
     def plain_big_step():
@@ -964,11 +984,13 @@ def run_batched(args, rank, world):
         "plain_sequential": {"value": plain_rate, "unit": "Msamples/s",
                              "what": "the same jobs as consecutive ct_render_image_device calls"},
         "speedup_vs_plain": value / plain_rate,
-        "ceiling_vs_plain": {"value": t_plain / t_big if t_big else None, "large_jobs": len(big),
-                             "large_job_samples": int(sum(jobs[k].width * jobs[k].height * spp for k in big)),
-                             "what": f"plain time of all jobs / plain time of the jobs of at least {FILL_PATHS} "
-                                     "paths, which fill the GPU alone: an upper bound of any batching's speedup "
-                                     "over the plain loop (it assumes the other jobs cost nothing)"},
+        "plain_large_jobs": {
+            "value": (sum(jobs[k].width * jobs[k].height * spp for k in big) * max(1, args.steps // 2) * world
+                      / t_big / 1e6) if t_big else None, "unit": "Msamples/s", "jobs": len(big),
+            "share_of_samples": sum(jobs[k].width * jobs[k].height * spp for k in big) / samples,
+            "share_of_plain_time": t_big / t_plain if t_big else None,
+            "what": f"the plain loop on the jobs of at least {FILL_PATHS} paths alone (they fill the GPU by "
+                    "themselves)"},
         "plain_per_frame": {"value": frame_rate, "unit": "Msamples/s",
                             "what": "the same jobs one after another, each as a progressive loop of one "
                                     "accumulatePass per frame (ct_accumulate_passes_device, passes = 1)"},
@@ -1079,8 +1101,8 @@ def run_served(args, rank, world):
     t_plain = max_over_ranks(t_plain, world, device)
     value = samples * args.steps * world / t_dev / 1e6
     plain_rate = samples * world / t_plain / 1e6
-    # Ceiling of any batching (as in the batched workload): the requests of at
-    # least FILL_PATHS paths rendered alone by the plain loop.
+    # The plain loop on the requests of at least FILL_PATHS paths alone (as in
+    # the batched workload).
     big = [r for r in trace if r.pixels * r.spp >= FILL_PATHS]
     t0 = time.perf_counter()
     render_plain(dev, at(big, None), opts, t0=t0)
@@ -1112,11 +1134,13 @@ def run_served(args, rank, world):
         "plain_sequential": {"value": plain_rate, "unit": "Msamples/s",
                              "what": "the same requests as consecutive ct_render_image_device calls, one at a time"},
         "speedup_vs_plain": value / plain_rate,
-        "ceiling_vs_plain": {"value": t_plain / t_big if t_big else None, "large_requests": len(big),
-                             "large_request_samples": int(sum(r.pixels * r.spp for r in big)),
-                             "what": f"plain time of all requests / plain time of the requests of at least "
-                                     f"{FILL_PATHS} paths, which fill the GPU alone: an upper bound of any "
-                                     "batching's speedup over the plain loop"},
+        "plain_large_requests": {
+            "value": sum(r.pixels * r.spp for r in big) * world / t_big / 1e6 if t_big else None,
+            "unit": "Msamples/s", "requests": len(big),
+            "share_of_samples": sum(r.pixels * r.spp for r in big) / samples,
+            "share_of_plain_time": t_big / t_plain if t_big else None,
+            "what": f"the plain loop on the requests of at least {FILL_PATHS} paths alone (they fill the GPU by "
+                    "themselves)"},
         "plain_per_frame": {"value": frame_rate, "unit": "Msamples/s",
                             "what": "the same requests one at a time, each as a progressive loop of one "
                                     "accumulatePass per frame (ct_accumulate_passes_device, passes = 1)"},

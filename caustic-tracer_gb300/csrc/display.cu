@@ -2,8 +2,12 @@
 // RGBA8 and a binary PPM (ppm.ts:4-16) straight from the sum buffer.
 //
 // Each channel is computed in float32 (ACES fit or Reinhard, then the sRGB
-// curve with powf); its scaled value y = 255 * srgb carries an error below
-// 3e-4. Only a channel whose y lies within 2e-3 of a rounding boundary
+// curve, whose power x^(1/2.4) is taken as exp2f(log2f(x) / 2.4)); its scaled
+// value y = 255 * srgb carries an error below 4e-4 (for x in [0.0031308, 1],
+// |log2 x| <= 8.33: log2f's 1 ulp is at most 9.6e-7, the division by 2.4 adds
+// 1 ulp of a value below 3.5, exp2f's 2 ulp add 2.4e-7 relative, so the power
+// is within 9e-7 relative and y within 255 * 1.055 * 9e-7 = 2.4e-4, plus the
+// roundings of the curve and of the scaling). Only a channel whose y lies within 2e-3 of a rounding boundary
 // (k + 0.5), or is not a number, is recomputed in float64 in the reference's
 // operation order, so every byte is the one the reference's float64 code
 // stores. One thread per pixel: 12 bytes read, 4 (or 3) written. The float64
@@ -54,7 +58,7 @@ __device__ float reinhard32(float x) { return x <= 0.0f ? 0.0f : x / (1.0f + x);
 __device__ float srgb32(float x) {
   if (x <= 0.0f) return 0.0f;
   if (x >= 1.0f) return 1.0f;
-  return x <= 0.0031308f ? 12.92f * x : __fmaf_rn(1.055f, powf(x, 1.0f / 2.4f), -0.055f);
+  return x <= 0.0031308f ? 12.92f * x : __fmaf_rn(1.055f, exp2f(log2f(x) * (1.0f / 2.4f)), -0.055f);
 }
 
 // The float32 byte of a channel; false when y is within kRoundMargin of a

@@ -18,6 +18,22 @@ namespace ct {
 namespace {
 
 constexpr uint64_t kMaxWavePaths = 8ull << 20;  // paths in flight per wave
+// Path-state sets of a render of several waves: wave k runs on set k % n, on
+// the caller's stream or one of the scene's side streams, so a wave's last
+// bounces overlap the next waves' first ones.
+constexpr int kRenderSets = 3;
+
+// The scene's side streams and events for renders of several waves.
+ct_status render_streams(ct_scene* s, int sets) {
+  for (int i = 0; i < sets - 1; i++) {
+    if (!s->render_side[i]) CT_CUDA(cudaStreamCreateWithFlags(&s->render_side[i], cudaStreamNonBlocking));
+    if (!s->render_join[i]) CT_CUDA(cudaEventCreateWithFlags(&s->render_join[i], cudaEventDisableTiming));
+  }
+  for (int i = 0; i < sets; i++)
+    if (!s->render_acc[i]) CT_CUDA(cudaEventCreateWithFlags(&s->render_acc[i], cudaEventDisableTiming));
+  if (!s->render_fork) CT_CUDA(cudaEventCreateWithFlags(&s->render_fork, cudaEventDisableTiming));
+  return CT_OK;
+}
 constexpr uint32_t kSkipMaxNodes = 31;         // trees this small use the stackless skip-link walk
 
 // Walk form of a scene's trace launches: the scene's CT_OPT_WALK when set,
@@ -50,44 +66,69 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
   const int32_t B = o.max_bounces;
   const int form = walk_form(s);
   const bool whole = whole_paths(s, form);
-  // Path buffer: 2 queues + shadow queue (3 float4 each per path), radiance
-  // (float4), hit prim/t, counters; k_paths needs the radiance and counters.
+  const uint64_t waves = (passes + per_wave - 1) / per_wave;
+  const int sets = whole ? 1 : (int)std::min<uint64_t>(kRenderSets, waves);
+  ct_status st;
+  if (sets > 1 && (st = render_streams(s, sets)) != CT_OK) return st;
+  // Path buffer per set: 2 queues + shadow queue (3 float4 each per path),
+  // radiance (float4), hit prim/t, counters; k_paths needs the radiance and
+  // counters.
   const size_t q_bytes = cap * sizeof(float4);
   const size_t counter_words = wave_counter_words(B);
-  const size_t bytes = (whole ? q_bytes : 10 * q_bytes + cap * 8) + counter_words * 4 + 16 * 256;
+  const size_t set_bytes = (whole ? q_bytes : 10 * q_bytes + cap * 8) + counter_words * 4 + 16 * 256;
   void* buf = nullptr;
-  ct_status st = path_alloc(s->device, bytes, stream, &buf);
+  st = path_alloc(s->device, set_bytes * (size_t)sets, stream, &buf);
   if (st != CT_OK) return st;
   struct Release {  // back to the pool, in stream order, on every return
     void* p;
     cudaStream_t s;
     ~Release() { path_free(p, s); }
   } release{buf, stream};
+  // The side streams join `stream` before the buffer goes back (declared
+  // after `release`, so it runs first), also on an early error return.
+  struct Join {
+    ct_scene* s;
+    cudaStream_t stream;
+    int sets;
+    bool forked = false;
+    ~Join() {
+      if (!forked) return;
+      for (int i = 0; i < sets - 1; i++) {
+        cudaEventRecord(s->render_join[i], s->render_side[i]);
+        cudaStreamWaitEvent(stream, s->render_join[i], 0);
+      }
+    }
+  } join{s, stream, sets};
   char* base = static_cast<char*>(buf);
   auto take = [&](size_t n) {
     char* p = base;
     base += (n + 255) & ~size_t(255);
     return p;
   };
-  WaveArgs a{};
-  a.scene = s->dev;
-  a.sky = to_sky(s->sky);
-  a.frame = to_frame(frame);
-  if (!whole) {
-    a.cur = Queue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes), nullptr};
-    a.next = Queue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes), nullptr};
-    a.shadow = ShadowQueue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes)};
-    a.hit_prim = (int32_t*)take(cap * 4);
-    a.hit_t = (float*)take(cap * 4);
+  WaveArgs set_args[kRenderSets];
+  for (int set = 0; set < sets; set++) {
+    WaveArgs& a = set_args[set];
+    a = WaveArgs{};
+    a.scene = s->dev;
+    a.sky = to_sky(s->sky);
+    a.frame = to_frame(frame);
+    if (!whole) {
+      a.cur = Queue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes), nullptr};
+      a.next = Queue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes), nullptr};
+      a.shadow = ShadowQueue{(float4*)take(q_bytes), (float4*)take(q_bytes), (float4*)take(q_bytes)};
+      a.hit_prim = (int32_t*)take(cap * 4);
+      a.hit_t = (float*)take(cap * 4);
+    }
+    a.radiance = (float4*)take(q_bytes);
+    a.counts = (uint32_t*)take(counter_words * 4);
+    a.width = width;
+    a.height = height;
+    a.pixels = (uint32_t)pixels;
+    a.max_bounces = B;
+    a.rr = o.russian_roulette;
+    a.nee = o.nee;
   }
-  a.radiance = (float4*)take(q_bytes);
-  a.counts = (uint32_t*)take(counter_words * 4);
-  a.width = width;
-  a.height = height;
-  a.pixels = (uint32_t)pixels;
-  a.max_bounces = B;
-  a.rr = o.russian_roulette;
-  a.nee = o.nee;
+  WaveArgs& a = set_args[0];
   const Grids<false>& g = grids<false>();
   if (whole) {
     for (uint64_t done = 0; done < passes; done += per_wave) {
@@ -107,33 +148,45 @@ ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, 
     }
     return CT_OK;
   }
-  auto trace = [&](const WaveArgs& w, int32_t b) {
-    ProfScope ps("trace", stream);
-    launch_trace<false>(form, w, b, stream, s->opt_trace_blocks);
-  };
-  for (uint64_t done = 0; done < passes; done += per_wave) {
+  if (sets > 1) {
+    CT_CUDA(cudaEventRecord(s->render_fork, stream));
+    for (int i = 0; i < sets - 1; i++) CT_CUDA(cudaStreamWaitEvent(s->render_side[i], s->render_fork, 0));
+    join.forked = true;
+  }
+  uint64_t k = 0;
+  for (uint64_t done = 0; done < passes; done += per_wave, k++) {
+    const int set = (int)(k % (uint64_t)sets);
+    const cudaStream_t st = set ? s->render_side[set - 1] : stream;
+    WaveArgs& wa = set_args[set];
     const uint32_t p = (uint32_t)std::min<uint64_t>(per_wave, passes - done);
-    a.paths = (uint32_t)(p * pixels);
-    a.first_frame = first + (uint32_t)done;
-    CT_CUDA(cudaMemsetAsync(a.counts, 0, counter_words * 4, stream));
+    wa.paths = (uint32_t)(p * pixels);
+    wa.first_frame = first + (uint32_t)done;
+    CT_CUDA(cudaMemsetAsync(wa.counts, 0, counter_words * 4, st));
     {
-      ProfScope ps("generate", stream);
-      k_generate<false><<<g.gen, kBlock, 0, stream>>>(a);
+      ProfScope ps("generate", st);
+      k_generate<false><<<g.gen, kBlock, 0, st>>>(wa);
     }
-    WaveArgs w = a;
+    WaveArgs w = wa;
+    auto trace = [&](int32_t b) {
+      ProfScope ps("trace", st);
+      launch_trace<false>(form, w, b, st, s->opt_trace_blocks);
+    };
     for (int32_t b = 0; b <= B; b++) {
-      trace(w, b);
+      trace(b);
       {
-        ProfScope ps("shade", stream);
-        k_shade<false><<<g.shade, kBlock, 0, stream>>>(w, b);
+        ProfScope ps("shade", st);
+        k_shade<false><<<g.shade, kBlock, 0, st>>>(w, b);
       }
       std::swap(w.cur, w.next);
     }
-    trace(w, B + 1);
+    trace(B + 1);
+    // pass order: this wave's samples are added after the previous wave's
+    if (sets > 1 && k > 0) CT_CUDA(cudaStreamWaitEvent(st, s->render_acc[(k - 1) % (uint64_t)sets], 0));
     {
-      ProfScope ps("accumulate", stream);
-      k_accumulate<<<g.acc, kBlock, 0, stream>>>(a.radiance, a.pixels, p, accum, sumsq);
+      ProfScope ps("accumulate", st);
+      k_accumulate<<<g.acc, kBlock, 0, st>>>(wa.radiance, wa.pixels, p, accum, sumsq);
     }
+    if (sets > 1) CT_CUDA(cudaEventRecord(s->render_acc[set], st));
     CT_CUDA(cudaGetLastError());
   }
   return CT_OK;

@@ -383,7 +383,13 @@ void destroy(ct_scene* s) {
   s->io.release(&s->device_bytes, s->stream);
   for (cudaStream_t c : {s->copy_in, s->copy_out, s->compute2})
     if (c) cudaStreamSynchronize(c), cudaStreamDestroy(c);
-  for (cudaEvent_t e : {s->ev_in, s->ev_done})
+  for (cudaStream_t c : s->render_side)
+    if (c) cudaStreamSynchronize(c), cudaStreamDestroy(c);
+  for (cudaEvent_t e : {s->ev_in, s->ev_done, s->render_fork})
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : s->render_join)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : s->render_acc)
     if (e) cudaEventDestroy(e);
   bool kept = false;
   if (s->stream && s->ev0 && s->ev1 && s->ev2 && s->device >= 0 && s->device < kPoolDevices &&

@@ -86,6 +86,11 @@ struct ct_scene {
   // and compute2 trace alternate chunks.
   cudaStream_t copy_in = nullptr, copy_out = nullptr, compute2 = nullptr;
   cudaEvent_t ev_in = nullptr, ev_done = nullptr;
+  // Streams and events of renders of several waves (created on the first
+  // one): consecutive waves run round robin on the caller's stream and these.
+  static constexpr int kRenderSides = 3;
+  cudaStream_t render_side[kRenderSides] = {};
+  cudaEvent_t render_fork = nullptr, render_join[kRenderSides] = {}, render_acc[kRenderSides + 1] = {};
 };
 
 namespace ct {

@@ -153,3 +153,32 @@ def test_render_sizes_and_waves(native_lib):
             frame = ct.camera_frame(sc.camera, w / h)
             img = ct.render_image(dev, frame, ct.RenderOptions(width=w, height=h, spp=2, seed=2))
             assert img.shape == (w * h * 3,) and np.isfinite(img).all()
+
+
+@pytest.mark.parametrize("scene_name", ["soup_sky", "caustic"])
+def test_waves_on_several_streams_sum_in_pass_order(native_lib, scene_name):
+    """A render split into many waves (consecutive waves on the caller's stream
+    and the scene's side streams, their path state in separate sets) equals the
+    same render in one wave bit for bit: every pixel's passes are still added
+    in pass order. Sums of squares too."""
+    import torch
+
+    sc = SCENES[scene_name]()
+    w, h, spp = 40, 24, 13
+    frame = ct.camera_frame(sc.camera, w / h)
+    o = _abi.ct_trace_options(8, 1, 1)
+    f = frame.struct()
+    with ct.DeviceScene.from_scene(sc) as dev:
+        outs = []
+        for wave_paths in (0, 2 * w * h, w * h):  # one wave; 7 waves of 2 passes; 13 waves of 1
+            _native.check(dev._lib.ct_scene_set_option(dev.handle, 2, wave_paths))
+            acc = torch.zeros(w * h * 3, device="cuda")
+            sq = torch.zeros(w * h * 3, device="cuda")
+            _native.check(dev._lib.ct_accumulate_passes_device(dev.handle, C.byref(f), w, h, 7919, spp, C.byref(o),
+                                                               _native.ptr(acc), _native.ptr(sq), None))
+            img = ct.render_image(dev, frame, ct.RenderOptions(width=w, height=h, spp=spp, seed=1))
+            torch.cuda.synchronize()
+            outs.append((acc.cpu().numpy(), sq.cpu().numpy(), img))
+    for got in outs[1:]:
+        for a, b in zip(outs[0], got):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
