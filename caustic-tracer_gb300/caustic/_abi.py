@@ -162,6 +162,7 @@ SIGNATURES = {
     "ct_batch_set_first_frames": (C.c_int, [P, C.POINTER(C.c_uint32)]),
     "ct_batch_run": (C.c_int, [P, P]),
     "ct_batch_run_direct": (C.c_int, [P, P]),
+    "ct_batch_run_direct_after": (C.c_int, [P, P, P]),
     "ct_batch_info": (C.c_int, [P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                 C.POINTER(C.c_int32)]),
     "ct_batch_destroy": (None, [P]),

@@ -308,10 +308,15 @@ def latency_stats(results: Sequence[Result]) -> dict:
 
 class GpuExecutor:
     """Executor on libcaustic_gb300: device-resident scenes and sum buffers, one
-    ct_batch per step launched without graph capture; finished images are read
-    back on a copy stream while the next step runs."""
+    ct_batch per step launched without graph capture. Consecutive steps run on
+    `streams` streams in turn, so a step's last bounces overlap the next
+    step's first ones; each step's sums are added after the previous step's
+    (ct_batch_run_direct_after), which keeps every request's passes in pass
+    order. Finished images are read back on a copy stream while the next step
+    runs."""
 
-    def __init__(self, scenes: Dict[str, DeviceScene], opts: TraceOptions, wave_paths: int = 0, stream=None):
+    def __init__(self, scenes: Dict[str, DeviceScene], opts: TraceOptions, wave_paths: int = 0, stream=None,
+                 streams: int = STEPS_IN_FLIGHT):
         import torch
 
         from . import _abi, _native
@@ -322,7 +327,10 @@ class GpuExecutor:
         self._lib = _native.lib()
         self._abi = _abi
         self._native = _native
-        self.stream = stream or torch.cuda.Stream()
+        self.stream = stream or torch.cuda.Stream()  # sum buffers are zeroed here; steps 0, n, 2n, ... run here
+        self.streams = [self.stream] + [torch.cuda.Stream() for _ in range(max(1, streams) - 1)]
+        self._turn = 0
+        self._last = None  # the previous step's batch (alive until the server waits for it)
         self.copy_stream = torch.cuda.Stream()
         self._topts = _abi.ct_trace_options(opts.max_bounces, int(opts.russian_roulette), int(opts.nee))
         self._bytes = {k: v.device_bytes for k, v in scenes.items()}
@@ -355,14 +363,21 @@ class GpuExecutor:
         handle = C.c_void_p()
         self._native.check(self._lib.ct_batch_create(arr, len(items), C.byref(self._topts), self.wave_paths, -1,
                                                      C.byref(handle)))
+        s = self.streams[self._turn % len(self.streams)]
+        if s is not self.stream:  # the sum buffers zeroed so far, before this step adds to them
+            s.wait_stream(self.stream)
         try:
-            self._native.check(self._lib.ct_batch_run_direct(handle, C.c_void_p(self.stream.cuda_stream)))
+            self._native.check(self._lib.ct_batch_run_direct_after(handle, C.c_void_p(s.cuda_stream), self._last))
         except Exception:
             self._lib.ct_batch_destroy(handle)
             raise
+        self._turn += 1
+        self._last = handle
         return handle
 
     def wait(self, handle) -> None:
+        if self._last is not None and self._last.value == handle.value:
+            self._last = None
         self._lib.ct_batch_destroy(handle)  # waits for the batch's run, recycles its buffers
 
     def fetch(self, req: Request, buf) -> np.ndarray:

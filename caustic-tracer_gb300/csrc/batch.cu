@@ -54,6 +54,7 @@ struct ct_batch {
   int nsets = 1;
   cudaStream_t side[kMaxSets] = {};  // streams of sets 1.. (set 0 runs on the caller's stream)
   cudaEvent_t fork = nullptr, join[kMaxSets] = {}, acc_done[kMaxSets] = {};
+  cudaEvent_t sums_done = nullptr;  // after the last accumulate of a direct run
   size_t counter_words = 0;
   bool segs_dirty = true;
   cudaGraph_t graph = nullptr;
@@ -148,8 +149,10 @@ void plan(ct_batch* b, uint64_t cap) {
 
 // Enqueues every wave of the batch on `s` (captured into the graph); with
 // several path-state sets, wave k runs on the stream of set k % nsets (set 0
-// on `s`, the others forked from and joined back into `s`).
-ct_status enqueue_all(ct_batch* b, cudaStream_t s) {
+// on `s`, the others forked from and joined back into `s`). Direct runs
+// (`direct`) record sums_done after the last accumulate, and with `after`
+// their first accumulate waits for that batch's sums_done.
+ct_status enqueue_all(ct_batch* b, cudaStream_t s, bool direct = false, const ct_batch* after = nullptr) {
   const Grids<true>& g = grids<true>();
   const int32_t B = b->opts.max_bounces;
   const int n = b->nsets;
@@ -175,10 +178,12 @@ ct_status enqueue_all(ct_batch* b, cudaStream_t s) {
       std::swap(w.cur, w.next);
     }
     launch_trace<true>(wv.walk, w, B + 1, st);
-    // pass order: wave k's sums are added after wave k-1's
+    // pass order: wave k's sums are added after wave k-1's (and wave 0's after `after`'s)
     if (n > 1 && k > 0) CT_CUDA(cudaStreamWaitEvent(st, b->acc_done[(k - 1) % (size_t)n], 0));
+    if (k == 0 && after && after->sums_done) CT_CUDA(cudaStreamWaitEvent(st, after->sums_done, 0));
     k_accumulate_batch<<<g.acc, kBlock, 0, st>>>(a);
     if (n > 1) CT_CUDA(cudaEventRecord(b->acc_done[set], st));
+    if (direct && k + 1 == b->waves.size()) CT_CUDA(cudaEventRecord(b->sums_done, st));
   }
   for (int i = 1; i < n; i++) {
     CT_CUDA(cudaEventRecord(b->join[i], b->side[i]));
@@ -202,6 +207,7 @@ void destroy(ct_batch* b) {
   if (b->d_paths) path_free(b->d_paths, b->stream);  // the runs are done: back to the pool at once
   if (b->done) cudaEventDestroy(b->done);
   if (b->fork) cudaEventDestroy(b->fork);
+  if (b->sums_done) cudaEventDestroy(b->sums_done);
   for (int i = 0; i < ct_batch::kMaxSets; i++) {
     if (b->join[i]) cudaEventDestroy(b->join[i]);
     if (b->acc_done[i]) cudaEventDestroy(b->acc_done[i]);
@@ -254,6 +260,11 @@ ct_status create(const ct_batch_job* jobs, uint32_t count, const ct_trace_option
     err = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
     if (err != cudaSuccess) {
       b->done = nullptr;
+      return bail(fail(CT_ERR_CUDA, "ct_batch_create: %s", cudaGetErrorString(err)));
+    }
+    err = cudaEventCreateWithFlags(&b->sums_done, cudaEventDisableTiming);
+    if (err != cudaSuccess) {
+      b->sums_done = nullptr;
       return bail(fail(CT_ERR_CUDA, "ct_batch_create: %s", cudaGetErrorString(err)));
     }
     b->nsets = (int)std::min<size_t>(std::min(kWaveSets, ct_batch::kMaxSets), std::max<size_t>(1, b->waves.size()));
@@ -325,7 +336,7 @@ ct_status create(const ct_batch_job* jobs, uint32_t count, const ct_trace_option
   return CT_OK;
 }
 
-ct_status run(ct_batch* b, cudaStream_t s, bool direct) {
+ct_status run(ct_batch* b, cudaStream_t s, bool direct, const ct_batch* after = nullptr) {
   CT_CUDA(cudaSetDevice(b->device));
   if (b->segs_dirty && !b->segs.empty()) {
     CT_CUDA(cudaMemcpyAsync(b->d_segs, b->segs.data(), b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, s));
@@ -334,7 +345,7 @@ ct_status run(ct_batch* b, cudaStream_t s, bool direct) {
   if (b->waves.empty()) return CT_OK;
   if (direct) {  // launches straight onto s (no capture): for one-shot batches
     ProfScope ps("batch_direct", s);
-    ct_status st = enqueue_all(b, s);
+    ct_status st = enqueue_all(b, s, true, after);
     if (st != CT_OK) return st;
     CT_CUDA(cudaEventRecord(b->done, s));
     return CT_OK;
@@ -399,6 +410,13 @@ ct_status ct_batch_run_direct(ct_batch* batch, void* stream) {
   ct::clear_error();
   CT_CHECK_ARG(batch != nullptr, "batch is NULL");
   return ct::run(batch, stream ? static_cast<cudaStream_t>(stream) : batch->stream, true);
+}
+
+ct_status ct_batch_run_direct_after(ct_batch* batch, void* stream, const ct_batch* after) {
+  ct::clear_error();
+  CT_CHECK_ARG(batch != nullptr, "batch is NULL");
+  CT_CHECK_ARG(after == nullptr || after->device == batch->device, "batches live on different devices");
+  return ct::run(batch, stream ? static_cast<cudaStream_t>(stream) : batch->stream, true, after);
 }
 
 ct_status ct_batch_info(const ct_batch* batch, uint32_t* waves, uint64_t* paths, uint64_t* graph_nodes,

@@ -309,6 +309,13 @@ ct_status ct_batch_run(ct_batch* batch, void* stream);
 /* Same work launched directly, without capturing a graph: for batches run
  * once (a serving step whose set of jobs changes every time).              */
 ct_status ct_batch_run_direct(ct_batch* batch, void* stream);
+/* ct_batch_run_direct whose sums are added only after those of the most
+ * recent run of `after` (NULL: none), which may run on another stream: two
+ * batches that add passes of the same jobs (consecutive serving steps) then
+ * overlap on the GPU while every pixel's passes stay in pass order. `after`
+ * must have been run and must not be destroyed before this call returns.
+ * No counterpart in the reference: accumulatePass (tracer.ts:361) in order. */
+ct_status ct_batch_run_direct_after(ct_batch* batch, void* stream, const ct_batch* after);
 ct_status ct_batch_info(const ct_batch* batch, uint32_t* waves, uint64_t* paths, uint64_t* graph_nodes,
                         int32_t* walk);
 void ct_batch_destroy(ct_batch* batch);
