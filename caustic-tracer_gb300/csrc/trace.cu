@@ -39,7 +39,9 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
   uint32_t fallbacks = 0;
   bool overflow = false;
   auto load = [&](uint32_t i, ctk::RayF& r) {
-    const float4 r0 = __ldg(rays + 2 * (size_t)i), r1 = __ldg(rays + 2 * (size_t)i + 1);
+    // rays and hits are touched once: streaming loads and stores keep them
+    // from evicting the tree's records from L1 (+0.4 %)
+    const float4 r0 = __ldcs(rays + 2 * (size_t)i), r1 = __ldcs(rays + 2 * (size_t)i + 1);
     r = ctk::RayF{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, 0.0f, 0.0f, 0.0f};
     ctk::finish_ray(r);
   };
@@ -49,13 +51,13 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
     if (ANY) {
       blocked[i] = h.prim >= 0 ? 1 : 0;
     } else {
-      prim[i] = h.prim;
+      __stcs(&prim[i], h.prim);
       float t = h.t;
       bool loose = h.err > ctk::kReportRel * h.t;
       // Without barycentrics, a loose triangle hit first tries the plane
       // distance (float32, bounded); k_refine takes what is still loose.
       if (!BARY && loose && h.prim >= 0 && ctk::plane_t(s, r, h.prim, ctk::kReportRel, t)) loose = false;
-      t_out[i] = h.prim < 0 ? INFINITY : (loose ? -h.t : t);
+      __stcs(&t_out[i], h.prim < 0 ? INFINITY : (loose ? -h.t : t));
       if (BARY && u_out) u_out[i] = h.prim >= 0 ? h.u : 0.0f;
       if (BARY && v_out) v_out[i] = h.prim >= 0 ? h.v : 0.0f;
     }

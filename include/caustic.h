@@ -199,7 +199,9 @@ void ct_scene_destroy(ct_scene* scene);
 /* Device bytes held by the scene (for admission budgets). Path state of a
  * render or batch is not part of it: it comes from a per-device
  * stream-ordered pool for the duration of the call's work, and the pool
- * keeps its high-water mark for reuse (8 Mi paths in flight ~ 1.5 GiB).     */
+ * keeps its high-water mark for reuse (168 bytes per path in flight: a
+ * render of several waves holds up to four sets of 16 Mi paths, 11 GiB; a
+ * batch of several waves up to four sets of 24 Mi, 17 GiB).                */
 uint64_t ct_scene_device_bytes(const ct_scene* scene);
 
 /* Per-scene tuning knobs, set by callers or an autotuner. No counterpart in
@@ -207,7 +209,7 @@ uint64_t ct_scene_device_bytes(const ct_scene* scene);
  *   CT_OPT_WALK        integrator trace walk: -1 chosen from the tree (default),
  *                      0 ordered walk per thread, 1 ordered walk with persistent
  *                      lane refill, 2 stackless skip-link walk (intersect.ts:290)
- *   CT_OPT_WAVE_PATHS  paths in flight per wave (0 = library default, 8 Mi)
+ *   CT_OPT_WAVE_PATHS  paths per wave (0 = library default, 16 Mi)
  *   CT_OPT_TRACE_BLOCKS  resident 128-thread blocks per SM of the integrator's
  *                      trace (or whole-path) launches of a single-scene render,
  *                      1..64, capped at the kernel's occupancy (0 = as many as
@@ -280,7 +282,8 @@ ct_status ct_render_image_device(ct_scene* scene, const ct_camera_frame* frame,
  * (tracer.ts:361-395) with frame indices first_frame_index + k, adding into
  * the job's device sum buffer `accum` (width*height*3 floats). Results equal
  * those of the single-scene entry points for the same frame indices.
- * The paths of all jobs share waves of up to wave_paths paths (0 = 8 Mi);
+ * The paths of all jobs share waves of up to wave_paths paths (0 = 24 Mi),
+ * up to four waves in flight on as many streams, added in pass order;
  * walk selects the trace walk: -1 = each job the walk its scene uses alone
  * (so every result equals its single-scene render bit for bit; a wave holds
  * jobs of one walk), or 0 ordered per thread, 1 ordered with persistent lane
