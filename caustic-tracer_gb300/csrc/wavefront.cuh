@@ -243,11 +243,11 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
   // Query i < n_ext: closest hit of path slot i; otherwise shadow ray i - n_ext.
   auto load = [&](uint32_t i, ctk::RayF& r) {
     if (i < n_ext) {
-      const float4 ra = a.cur.a[i], rb = a.cur.b[i];
+      const float4 ra = __ldcs(&a.cur.a[i]), rb = __ldcs(&a.cur.b[i]);  // streamed: touched once
       r = ctk::RayF{ra.x, ra.y, ra.z, rb.x, rb.y, rb.z, ctk::kTMin, INFINITY, 0.0f, 0.0f, 0.0f};
     } else {
       const uint32_t j = i - n_ext;
-      const float4 sa = a.shadow.a[j], sb = a.shadow.b[j];
+      const float4 sa = __ldcs(&a.shadow.a[j]), sb = __ldcs(&a.shadow.b[j]);
       r = ctk::RayF{sa.x, sa.y, sa.z, sb.x, sb.y, sb.z, ctk::kTMin, sa.w, 0.0f, 0.0f, 0.0f};
     }
     ctk::finish_ray(r);
@@ -257,8 +257,8 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
   };
   auto finish = [&](uint32_t i, ctk::Walk& w) {
     if (i < n_ext) {
-      a.hit_prim[i] = w.h.prim;
-      a.hit_t[i] = w.h.t;
+      __stcs(&a.hit_prim[i], w.h.prim);
+      __stcs(&a.hit_t[i], w.h.t);
     } else if (w.h.prim < 0) {  // unoccluded: add the NEE contribution
       const uint32_t j = i - n_ext;
       const float4 c = a.shadow.c[j];

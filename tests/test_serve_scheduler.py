@@ -110,7 +110,7 @@ def test_small_requests_finish_while_a_large_one_continues():
     srv.submit(_req(0, 256, 64))
     srv.step()
     srv.submit(_req(1, 32, 2))  # arrives while the large request is in flight
-    for _ in range(3):
+    for _ in range(STEPS_IN_FLIGHT + 1):
         srv.step()
     done = {r.request.rid for r in srv.results}
     assert 1 in done and 0 not in done  # continuous batching: joined and left mid-flight
@@ -123,10 +123,11 @@ def test_steps_are_pipelined_and_bounded():
     srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=step_paths, min_chunk_paths=0, clock=Clock())
     for i in range(20):
         srv.submit(_req(i, 64, 5))
+    for k in range(1, STEPS_IN_FLIGHT):
+        srv.step()
+        assert ex.pending == k  # launched, not waited for
     srv.step()
-    assert ex.pending == 1  # launched, not waited for
-    srv.step()
-    assert ex.pending == STEPS_IN_FLIGHT - 1
+    assert ex.pending == STEPS_IN_FLIGHT - 1  # the oldest completed once the pipeline was full
     srv.drain()
     # every step fits in step_paths paths (one wave)
     for items in ex.steps:
