@@ -13,6 +13,7 @@
 #include <cstring>
 #include <limits>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include <cuda_fp16.h>
@@ -110,8 +111,6 @@ bool is_index(float f, uint32_t limit) {
 ct_status check_tree(const ct_packed_scene_view& v, uint32_t* interior_count, uint32_t* depth_out) {
   const float* n = v.nodes;
   const uint32_t N = v.node_count;
-  for (size_t i = 0; i < (size_t)N * CT_NODE_STRIDE; i++)
-    if (!std::isfinite(n[i])) return fail(CT_ERR_INVALID_ARGUMENT, "nodes[%zu] is not finite", i);
   uint32_t interior = 0, depth = 0;
   // Explicit post-order walk: frame = (node, depth, stage, end of left subtree).
   struct F {
@@ -265,15 +264,34 @@ std::vector<uint4> half_records(const std::vector<float4>& recs) {
     const __half hb = up ? __float2half_ru(b) : __float2half_rd(b);
     return (uint32_t)__half_as_ushort(ha) | ((uint32_t)__half_as_ushort(hb) << 16);
   };
-  for (size_t r = 0; r < R; r++) {
-    const float4* q = &recs[r * 8];
-    for (int a = 0; a < 3; a++) {
-      const float4 lo = q[2 * a], hi = q[2 * a + 1];
-      out[r * 4 + a] = make_uint4(pair(lo.x, lo.y, false), pair(lo.z, lo.w, false), pair(hi.x, hi.y, true),
-                                  pair(hi.z, hi.w, true));
+  auto range = [&](size_t r0, size_t r1) {
+    for (size_t r = r0; r < r1; r++) {
+      const float4* q = &recs[r * 8];
+      for (int a = 0; a < 3; a++) {
+        const float4 lo = q[2 * a], hi = q[2 * a + 1];
+        out[r * 4 + a] = make_uint4(pair(lo.x, lo.y, false), pair(lo.z, lo.w, false), pair(hi.x, hi.y, true),
+                                    pair(hi.z, hi.w, true));
+      }
+      std::memcpy(&out[r * 4 + 3], &q[6], sizeof(uint4));
     }
-    std::memcpy(&out[r * 4 + 3], &q[6], sizeof(uint4));
+  };
+  // Large trees: four threads, each a contiguous quarter of the records.
+  constexpr size_t kThreadedRecords = 16384;
+  std::thread parts[3];
+  size_t done = 0;
+  if (R >= kThreadedRecords) {
+    const size_t q = R / 4;
+    try {
+      for (int i = 0; i < 3; i++) {
+        parts[i] = std::thread(range, (size_t)i * q, (size_t)(i + 1) * q);
+        done = (size_t)(i + 1) * q;
+      }
+    } catch (const std::exception&) {  // no more threads: this thread takes the rest
+    }
   }
+  range(done, R);
+  for (std::thread& t : parts)
+    if (t.joinable()) t.join();
   return out;
 }
 
@@ -322,7 +340,8 @@ std::vector<float4> plane_records(const ct_packed_scene_view& v) {
   return out;
 }
 
-ct_status validate_view(const ct_packed_scene_view& v) {
+// The arrays are present and their counts within the encodings' limits.
+ct_status validate_pointers(const ct_packed_scene_view& v) {
   CT_CHECK_ARG(v.node_count == 0 || v.nodes != nullptr, "nodes is NULL");
   CT_CHECK_ARG(v.prim_count == 0 || v.prims != nullptr, "prims is NULL");
   CT_CHECK_ARG(v.prim_count == 0 || v.prim_object != nullptr, "prim_object is NULL");
@@ -330,6 +349,14 @@ ct_status validate_view(const ct_packed_scene_view& v) {
   CT_CHECK_ARG(v.mats != nullptr || v.prim_count == 0, "mats is NULL");
   CT_CHECK_ARG(v.prim_count < (1u << 21), "prim_count %u exceeds the float32 leaf encoding", v.prim_count);
   CT_CHECK_ARG(v.node_count < (1u << 24), "node_count %u exceeds the float32 skip encoding", v.node_count);
+  return CT_OK;
+}
+
+// The values of the node, primitive, material and light arrays and the sky
+// (the tree's links are checked by check_tree).
+ct_status validate_view(const ct_packed_scene_view& v) {
+  for (size_t i = 0; i < (size_t)v.node_count * CT_NODE_STRIDE; i++)
+    if (!std::isfinite(v.nodes[i])) return fail(CT_ERR_INVALID_ARGUMENT, "nodes[%zu] is not finite", i);
   const uint32_t mat_records = v.mat_count > 0 ? v.mat_count : 1;
   for (uint32_t p = 0; p < v.prim_count; p++) {
     const float* q = v.prims + (size_t)p * CT_PRIM_STRIDE;
@@ -365,7 +392,8 @@ ct_status upload(ct_scene* s, DeviceBuffer& b, char*& cursor, const T* src, size
   b.ptr = cursor;
   b.bytes = n * sizeof(T);
   cursor += arena_slot(b.bytes);
-  CT_CUDA(cudaMemsetAsync(b.ptr, 0, n * sizeof(T), s->stream));
+  if (n > count)  // only the padding past the copied elements starts at zero
+    CT_CUDA(cudaMemsetAsync(static_cast<char*>(b.ptr) + count * sizeof(T), 0, (n - count) * sizeof(T), s->stream));
   if (count) CT_CUDA(cudaMemcpyAsync(b.ptr, src, count * sizeof(T), cudaMemcpyHostToDevice, s->stream));
   return CT_OK;
 }
@@ -414,9 +442,49 @@ void destroy(ct_scene* s) {
   delete s;
 }
 
+// Scenes of at least this many primitives run their independent host passes
+// on separate threads (caustic scene, 327,746 primitives: the create call's
+// host work drops to the tree check and record build; below this size the
+// threads cost more than they save).
+constexpr uint32_t kThreadedPrims = 50000;
+
 ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
-  ct_status st = validate_view(v);
+  ct_status st = validate_pointers(v);
   if (st != CT_OK) return st;
+  // The value checks and the plane records read only the primitive,
+  // material and light arrays, so they run beside the tree check, the
+  // record build and the half records (which follow the check).
+  const bool threaded = v.prim_count >= kThreadedPrims;
+  ct_status values = CT_OK;
+  std::vector<float4> planes;
+  bool planes_oom = false;
+  auto plane_pass = [&] {
+    try {
+      planes = plane_records(v);
+    } catch (const std::bad_alloc&) {
+      planes_oom = true;
+    }
+  };
+  std::thread t_values, t_planes;
+  if (threaded) {
+    try {
+      t_values = std::thread([&] { values = validate_view(v); });
+      t_planes = std::thread(plane_pass);
+    } catch (const std::exception&) {  // no threads: the passes run on this thread below
+    }
+  }
+  struct Joiner {  // every return below joins the worker threads first
+    std::thread& a;
+    std::thread& b;
+    ~Joiner() {
+      if (a.joinable()) a.join();
+      if (b.joinable()) b.join();
+    }
+  } joiner{t_values, t_planes};
+  if (!t_values.joinable()) {
+    st = validate_view(v);
+    if (st != CT_OK) return st;
+  }
   uint32_t interior = 0, depth = 0;
   if (v.node_count > 0) {
     st = check_tree(v, &interior, &depth);
@@ -426,14 +494,23 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   int32_t root_ref = ~0;
   uint32_t stack_need = 0;
   std::vector<uint4> halves;
-  std::vector<float4> planes;
   try {
     build_quads(v, quads, &root_ref, &stack_need);
     halves = half_records(quads);
-    planes = plane_records(v);
   } catch (const std::bad_alloc&) {
     return fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");
   }
+  if (t_values.joinable()) {
+    t_values.join();
+    // the error message belongs to the calling thread: run the check again here
+    if (values != CT_OK) return validate_view(v);
+  }
+  if (t_planes.joinable()) {
+    t_planes.join();
+  } else {
+    plane_pass();
+  }
+  if (planes_oom) return fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");
 
   ct_scene* s = new (std::nothrow) ct_scene();
   if (!s) return fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");

@@ -96,3 +96,32 @@ def test_scene_create_rejects_malformed_arrays(native_lib):
     v2 = bad2.view()
     assert native_lib.ct_scene_create(C.byref(v2), C.byref(h)) == 1
     assert b"skip" in native_lib.ct_last_error()
+
+
+def test_large_scene_validation_on_worker_threads_reports_here(native_lib):
+    """Scenes of 50,000 primitives or more check their values on worker threads
+    beside the tree check; a failure still comes back as this call's status and
+    this thread's ct_last_error message (no device needed)."""
+    import ctypes as C
+
+    import caustic as ct
+
+    ps = ct.pack_scene(ct.triangle_soup(60_000, seed=3))
+    h = C.c_void_p()
+    cases = []
+    prims = ps.prims.copy()
+    prims[16 * 1234 + 5] = np.nan
+    cases.append((ct.PackedScene(prims, ps.prim_count, ps.nodes, ps.node_count, ps.mats, ps.mat_count, ps.lights,
+                                 ps.prim_object, ps.sky, ps.order), b"non-finite"))
+    nodes = ps.nodes.copy()
+    nodes[8 * 77 + 1] = np.inf
+    cases.append((ct.PackedScene(ps.prims, ps.prim_count, nodes, ps.node_count, ps.mats, ps.mat_count, ps.lights,
+                                 ps.prim_object, ps.sky, ps.order), b"not finite"))
+    obj = ps.prim_object.copy()
+    obj[59_999] = 7
+    cases.append((ct.PackedScene(ps.prims, ps.prim_count, ps.nodes, ps.node_count, ps.mats, ps.mat_count, ps.lights,
+                                 obj, ps.sky, ps.order), b"prim_object"))
+    for bad, msg in cases:
+        v = bad.view()
+        assert native_lib.ct_scene_create(C.byref(v), C.byref(h)) == 1
+        assert msg in native_lib.ct_last_error(), native_lib.ct_last_error()
