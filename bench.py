@@ -17,7 +17,9 @@ Workloads
             device (ct_tonemap_device). Metric: Mpixels/s.
 
 The default line (cornell) also carries the traversal and caustic workloads
-as sub-records, each with its own value, roofline, CPU baseline and e2e.
+as sub-records, each with its own value, roofline, CPU baseline and e2e, and
+the batched and served forms (5 and 2 timed steps) with their plain
+baselines.
 
 `value` is device time with inputs resident in HBM (CUDA events on the
 launching stream, max over ranks); `e2e` is the same metric through the
@@ -514,11 +516,19 @@ SUB_KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step
 
 
 def default_line(args) -> bool:
-    """The default run (the Cornell headline) also measures traversal and caustic."""
+    """The default run (the Cornell headline) also measures traversal, caustic,
+    batched and served."""
     return args.workload == "cornell" and not args.small and not args.headline_only
 
 
+BATCH_KEYS = ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config", "clocks", "gpu_launches",
+              "plain_sequential", "speedup_vs_plain", "plain_per_frame", "speedup_vs_per_frame", "plain_large_jobs",
+              "plain_large_requests", "latency", "e2e")
+
+
 def run_gpu(args, rank, world):
+    import copy
+
     import torch
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
@@ -527,6 +537,14 @@ def run_gpu(args, rank, world):
         for sub in SUB_WORKLOADS:
             rec = measure(sub, args, rank, world, args.steps, args.warmup, headline=False)
             line[sub] = {k: rec[k] for k in SUB_KEYS if k in rec}
+        # the batched and served forms (BASELINE configs 4 and 5), fewer steps each
+        sub_args = copy.copy(args)
+        sub_args.steps, sub_args.warmup = max(1, min(args.steps, 5)), min(args.warmup, 3)
+        rec = run_batched(sub_args, rank, world, emit=False)
+        line["batched"] = {k: rec[k] for k in BATCH_KEYS if k in rec}
+        sub_args.steps, sub_args.trace = max(1, min(args.steps, 2)), "c5"
+        rec = run_served(sub_args, rank, world, emit=False)
+        line["served"] = {k: rec[k] for k in BATCH_KEYS if k in rec}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -899,7 +917,7 @@ def batched_inputs(count: int, small: bool):
     return [(p, ct.camera_frame(s.camera, w / h), w, h) for p, (s, w, h) in zip(packed, spec)]
 
 
-def run_batched(args, rank, world):
+def run_batched(args, rank, world, emit=True):
     """Batched form: all jobs in one graph launch vs the same jobs as sequential plain renders."""
     import torch
 
@@ -1025,8 +1043,9 @@ def run_batched(args, rank, world):
     br.close()
     for d in scenes:
         d.close()
-    if rank == 0:
+    if emit and rank == 0:
         print(json.dumps(line), flush=True)
+    return line
 
 
 def served_inputs(count: int, small: bool, rank: int, trace: str = "c5"):
@@ -1054,7 +1073,7 @@ def served_inputs(count: int, small: bool, rank: int, trace: str = "c5"):
     return packed, reqs
 
 
-def run_served(args, rank, world):
+def run_served(args, rank, world, emit=True):
     """Served form: a request trace through the continuous-batching server
     against the same trace as one plain renderImage per request, first all
     queued at once (throughput), then with Poisson arrivals (latency)."""
@@ -1175,8 +1194,9 @@ def run_served(args, rank, world):
     }
     for d in dev.values():
         d.close()
-    if rank == 0:
+    if emit and rank == 0:
         print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
