@@ -676,11 +676,13 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
 // lanes keep stepping instead of waiting for the warp's slowest ray (6 suits
 // the exact query walk, 0.7 % ahead of 8; 12 the integrator's, 1.7 % ahead
 // of 16 on the batched soups and 0.5 % behind it on the caustic scene). Each round of the
-// loop takes two steps per lane, which halves the refill bookkeeping (one
-// step per round ran 5 % slower on the 1M-triangle query walk, three or four
-// 20-35 % slower). With PHASED, the second step of a round moves either the
-// lanes testing primitives or those expanding records, whichever are more, so each branch
-// runs with fuller warps; every lane still makes its own tests in the same
+// exact walk takes two steps per lane, which halves the refill bookkeeping
+// (one step per round ran 5 % slower on the 1M-triangle query walk, three or
+// four 20-35 % slower); the integrator's walk, whose steps test whole leaves,
+// takes three (batched soups +2.3 %, a 100k soup +1.5 %, the caustic scene
+// unchanged; one step per round: 8 % slower). With PHASED, the steps after
+// the first move either the lanes testing primitives or those expanding
+// records, whichever are more, so each branch runs with fuller warps; every lane still makes its own tests in the same
 // order (measured: 1.5 % faster for the integrator's walk, 4 % slower for the
 // exact query walk). All 32 lanes of every warp must call this (the block
 // size is a multiple of 32).
@@ -725,6 +727,15 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
       go = go && (w.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
     }
     if (go) walk_step<EXACT>(s, w, fallbacks);
+    if (!EXACT) {  // the integrator's walk takes a third step, gated the same way
+      bool go3 = w.ref != kWalkDone;
+      if (PHASED) {
+        const uint32_t leaf = __ballot_sync(0xffffffffu, w.ref == kWalkLeaf);
+        const uint32_t inner = __ballot_sync(0xffffffffu, w.ref >= 0);
+        go3 = go3 && (w.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
+      }
+      if (go3) walk_step<EXACT>(s, w, fallbacks);
+    }
   }
 }
 
