@@ -7,15 +7,17 @@
 // |log2 x| <= 8.33: log2f's 1 ulp is at most 9.6e-7, the division by 2.4 adds
 // 1 ulp of a value below 3.5, exp2f's 2 ulp add 2.4e-7 relative, so the power
 // is within 9e-7 relative and y within 255 * 1.055 * 9e-7 = 2.4e-4, plus the
-// roundings of the curve and of the scaling). Only a channel whose y lies within 2e-3 of a rounding boundary
-// (k + 0.5), or is not a number, is recomputed in float64 in the reference's
-// operation order, so every byte is the one the reference's float64 code
-// stores. One thread per pixel: 12 bytes read, 4 (or 3) written. The float64
-// recomputations (about 0.4 % of channels) do not run where they arise: a
-// thread queues the channel in its block's shared memory and stores a
-// provisional byte, and the block later recomputes its queue with every lane
-// busy, so the slow float64 unit never runs with one lane of a warp active
-// while the other 31 wait.
+// roundings of the curve and of the scaling). Only a channel whose y lies
+// within 1e-3 of a rounding boundary (k + 0.5), or is not a number, is
+// recomputed in float64 in the reference's operation order (its power as
+// exp(log(x) / 2.4), within about 1e-15 relative of the exact power), so
+// every byte is the one the reference's float64 code stores unless y lies
+// within about 1e-12 of a boundary. One thread per pixel: 12 bytes read, 4
+// (or 3) written. The float64 recomputations (about 0.2 % of channels) do not
+// run where they arise: a thread queues the channel in its block's shared
+// memory and stores a provisional byte, and the block later recomputes its
+// queue with every lane busy, so the slow float64 unit never runs with one
+// lane of a warp active while the other 31 wait.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -26,7 +28,7 @@
 namespace ct {
 namespace {
 
-constexpr float kRoundMargin = 2e-3f;
+constexpr float kRoundMargin = 1e-3f;
 constexpr int kBlock = 256;
 
 // tonemap.ts:7-15 and 18-20, float64
@@ -39,7 +41,7 @@ __device__ double reinhard64(double x) { return x <= 0 ? 0 : x / (1 + x); }
 __device__ double srgb64(double x) {
   if (x <= 0) return 0;
   if (x >= 1) return 1;
-  return x <= 0.0031308 ? 12.92 * x : 1.055 * pow(x, 1 / 2.4) - 0.055;
+  return x <= 0.0031308 ? 12.92 * x : 1.055 * exp(log(x) / 2.4) - 0.055;
 }
 // Math.round (halves toward +infinity), then the Uint8ClampedArray store
 // (clamp to [0, 255], NaN -> 0).
