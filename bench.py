@@ -534,17 +534,25 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     line = measure(args.workload, args, rank, world, args.steps, args.warmup, headline=True)
     if default_line(args):
+        # A sub-record that fails is reported as such; the headline line is printed regardless.
+        def sub_record(name, fn, keys):
+            try:
+                rec = fn()
+                line[name] = {k: rec[k] for k in keys if k in rec}
+            except Exception as exc:  # noqa: BLE001
+                line[name] = {"error": f"{type(exc).__name__}: {exc}"[:500]}
+                torch.cuda.synchronize()
+
         for sub in SUB_WORKLOADS:
-            rec = measure(sub, args, rank, world, args.steps, args.warmup, headline=False)
-            line[sub] = {k: rec[k] for k in SUB_KEYS if k in rec}
+            sub_record(sub, lambda sub=sub: measure(sub, args, rank, world, args.steps, args.warmup, headline=False),
+                       SUB_KEYS)
         # the batched and served forms (BASELINE configs 4 and 5), fewer steps each
-        sub_args = copy.copy(args)
-        sub_args.steps, sub_args.warmup = max(1, min(args.steps, 5)), min(args.warmup, 3)
-        rec = run_batched(sub_args, rank, world, emit=False)
-        line["batched"] = {k: rec[k] for k in BATCH_KEYS if k in rec}
-        sub_args.steps, sub_args.trace = max(1, min(args.steps, 2)), "c5"
-        rec = run_served(sub_args, rank, world, emit=False)
-        line["served"] = {k: rec[k] for k in BATCH_KEYS if k in rec}
+        b_args = copy.copy(args)
+        b_args.steps, b_args.warmup = max(1, min(args.steps, 5)), min(args.warmup, 3)
+        sub_record("batched", lambda: run_batched(b_args, rank, world, emit=False), BATCH_KEYS)
+        s_args = copy.copy(b_args)
+        s_args.steps, s_args.trace = max(1, min(args.steps, 2)), "c5"
+        sub_record("served", lambda: run_served(s_args, rank, world, emit=False), BATCH_KEYS)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
