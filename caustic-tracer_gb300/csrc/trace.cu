@@ -77,10 +77,11 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
   } else if (VARIANT == 2) {  // the ordered walk, one query per thread
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-      ctk::Walk w;
+      ctk::WalkFrame f;
+      ctk::Walk& w = f.w;
       load(i, w.r);
       ctk::walk_begin(s, w, ANY);
-      while (w.ref != ctk::kWalkDone) ctk::walk_step<true>(s, w, fallbacks);
+      while (w.ref != ctk::kWalkDone) ctk::walk_step<true>(s, w, f.st, fallbacks);
       overflow |= w.overflow;
       store(i, w.r, w.h);
     }

@@ -556,7 +556,26 @@ struct Walk {
   uint32_t cur, end;
   int32_t sp;
   bool any, overflow;
-  int2 stack[kStackSize];  // (child reference, entry distance bits): one 8-byte access per push or pop
+};
+
+// The walk stack: (child reference, entry distance bits), one 8-byte access
+// per push or pop, in local memory.
+struct WalkStack {
+  int2 e[kStackSize];
+};
+
+// A walk's state and stack as one object. An array indexed at run time keeps
+// its whole enclosing object in local memory, so in a WalkFrame the ray, hit
+// and counters live in local memory beside the stack (read back from L1);
+// a Walk declared apart from its WalkStack is kept in registers. Measured on
+// GB300: the exact query walk (1M-triangle soup, 16.7 M rays, 40 registers)
+// runs at 894 Mrays/s with a WalkFrame against 761 with the state apart
+// (where the compiler spills it; 786 with only the hit in local memory, 748
+// with only the ray), while the integrator's walk gains with its state
+// apart (caustic scene 1,822 -> 1,914 Msamples/s, 100k soup 499 -> 526).
+struct WalkFrame {
+  Walk w;
+  WalkStack st;
 };
 
 constexpr int32_t kWalkPop = INT32_MAX, kWalkDone = INT32_MIN, kWalkLeaf = INT32_MIN + 1;
@@ -597,7 +616,7 @@ __device__ __forceinline__ void walk_enter(Walk& w, int32_t c) {
 // (caustic scene: 1,067 -> 1,214 Msamples/s, identical images; the exact
 // walk with whole-leaf steps ran at 645 against 895 Mrays/s).
 template <bool EXACT>
-__device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& fallbacks) {
+__device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack& st, uint32_t& fallbacks) {
   if (w.ref == kWalkLeaf) {
     if constexpr (EXACT) {
       if (test_prim<EXACT>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
@@ -649,9 +668,9 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
       w.ref = kWalkDone;
       return;
     } else {
-      if (hits > 3) w.stack[w.sp++] = make_int2(c3, __float_as_int(t3));
-      if (hits > 2) w.stack[w.sp++] = make_int2(c2, __float_as_int(t2));
-      if (hits > 1) w.stack[w.sp++] = make_int2(c1, __float_as_int(t1));
+      if (hits > 3) st.e[w.sp++] = make_int2(c3, __float_as_int(t3));
+      if (hits > 2) st.e[w.sp++] = make_int2(c2, __float_as_int(t2));
+      if (hits > 1) st.e[w.sp++] = make_int2(c1, __float_as_int(t1));
       walk_enter(w, c0);
     }
   }
@@ -660,7 +679,7 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, uint32_t& 
     const float bound = prune_bound(w.h);
     while (w.sp > 0) {
       --w.sp;
-      const int2 e = w.stack[w.sp];
+      const int2 e = st.e[w.sp];
       if (__int_as_float(e.y) <= bound) {
         walk_enter(w, e.x);
         break;
@@ -693,7 +712,11 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
                                                 Finish finish, uint32_t& fallbacks) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  Walk w;
+  WalkFrame frame;             // the exact walk: state beside the stack
+  Walk apart;                  // the integrator's walk: state in registers
+  WalkStack apart_stack;
+  Walk& w = EXACT ? frame.w : apart;
+  WalkStack& st = EXACT ? frame.st : apart_stack;
   w.ref = kWalkDone;
   int64_t idx = -1;  // query held by this lane
   bool drained = false;
@@ -719,14 +742,14 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
       }
     }
     if (__all_sync(0xffffffffu, idx < 0) && drained) break;
-    if (w.ref != kWalkDone) walk_step<EXACT>(s, w, fallbacks);
+    if (w.ref != kWalkDone) walk_step<EXACT>(s, w, st, fallbacks);
     bool go = w.ref != kWalkDone;
     if (PHASED) {
       const uint32_t leaf = __ballot_sync(0xffffffffu, w.ref == kWalkLeaf);
       const uint32_t inner = __ballot_sync(0xffffffffu, w.ref >= 0);
       go = go && (w.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
     }
-    if (go) walk_step<EXACT>(s, w, fallbacks);
+    if (go) walk_step<EXACT>(s, w, st, fallbacks);
     if (!EXACT) {  // the integrator's walk takes a third step, gated the same way
       bool go3 = w.ref != kWalkDone;
       if (PHASED) {
@@ -734,21 +757,9 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
         const uint32_t inner = __ballot_sync(0xffffffffu, w.ref >= 0);
         go3 = go3 && (w.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
       }
-      if (go3) walk_step<EXACT>(s, w, fallbacks);
+      if (go3) walk_step<EXACT>(s, w, st, fallbacks);
     }
   }
-}
-
-// Complete walk of one query in the calling thread (no refill).
-template <bool EXACT>
-__device__ __forceinline__ bool walk_ordered(const SceneDev& s, const RayF& r, HitF& h, bool any,
-                                             uint32_t& fallbacks) {
-  Walk w;
-  w.r = r;
-  walk_begin(s, w, any);
-  while (w.ref != kWalkDone) walk_step<EXACT>(s, w, fallbacks);
-  h = w.h;
-  return !w.overflow;
 }
 
 // Scenes of at most kBrutePrims primitives: every primitive tested in packed

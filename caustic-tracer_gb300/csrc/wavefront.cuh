@@ -295,6 +295,7 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_ext + n_sh; i += stride) {
       ctk::Walk w;
+      ctk::WalkStack st;
       load(i, w.r);
       const ctk::SceneDev sc = BATCH ? job_of(i).scene : a.scene;
       if constexpr (FORM == kWalkSkip) {
@@ -305,7 +306,7 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
           ctk::walk_stackless<false>(sc, w.r, w.h, i >= n_ext, fallbacks);
       } else {
         ctk::walk_begin(sc, w, i >= n_ext);
-        while (w.ref != ctk::kWalkDone) ctk::walk_step<false>(sc, w, fallbacks);
+        while (w.ref != ctk::kWalkDone) ctk::walk_step<false>(sc, w, st, fallbacks);
       }
       finish(i, w);
     }
