@@ -49,7 +49,9 @@ struct SceneDev {
   float root_lo[3], root_hi[3];
 };
 
-struct RayF {
+// 16-byte aligned: where a ray sits in local memory (the exact walk's
+// WalkFrame), its fields load as 16-byte vectors.
+struct alignas(16) RayF {
   float ox, oy, oz, dx, dy, dz, tmin, tmax;
   float ix, iy, iz;  // safe inverse direction (intersect.ts:142)
 };
@@ -549,12 +551,12 @@ __device__ __forceinline__ float prune_bound(const HitF& h) { return h.t + h.err
 // others pushed farthest first with their entry distances), tests one
 // primitive of the current leaf, or pops the stack past entries beyond the
 // closest hit. Equal-cost steps keep the lanes of a warp in step.
-struct Walk {
-  RayF r;
-  HitF h;
-  int32_t ref;           // >= 0 interior record, kLeaf: testing [cur, end), kPop, kDone
+struct alignas(16) Walk {
+  int32_t ref;  // >= 0 interior record, kLeaf: testing [cur, end), kPop, kDone
   uint32_t cur, end;
   int32_t sp;
+  RayF r;
+  HitF h;
   bool any, overflow;
 };
 
@@ -573,6 +575,8 @@ struct WalkStack {
 // (where the compiler spills it; 786 with only the hit in local memory, 748
 // with only the ray), while the integrator's walk gains with its state
 // apart (caustic scene 1,822 -> 1,914 Msamples/s, 100k soup 499 -> 526).
+// With the ray and the frame 16-byte aligned (the counters first, then the
+// ray's three 16-byte groups) the exact walk runs at 912 against 896.
 struct WalkFrame {
   Walk w;
   WalkStack st;
