@@ -462,8 +462,10 @@ __device__ __forceinline__ bool sphere_fast(const RayF& r, float4 c4, float rad,
 // the bounds are small (a tie within 1e-5), the float32 order decides;
 // otherwise both distances are recomputed in float64 and compared exactly
 // like the reference. Otherwise: plain float32 tests and comparisons.
-// any: returns true for any candidate (occlusion).
-template <bool EXACT>
+// any: returns true for any candidate (occlusion). UV: keep the closest
+// hit's barycentrics (the exact walk skips them when the caller does not ask
+// for them: two divisions per candidate and two stores to the walk frame).
+template <bool EXACT, bool UV = true>
 __device__ __forceinline__ bool test_prim(const SceneDev& s, const RayF& r, uint32_t p, HitF& h, bool any,
                                           uint32_t& fallbacks) {
   Cand c;
@@ -513,8 +515,10 @@ __device__ __forceinline__ bool test_prim(const SceneDev& s, const RayF& r, uint
     h.prim = (int32_t)p;
     h.t = c.t;
     h.err = c.e;
-    h.u = c.u;
-    h.v = c.v;
+    if constexpr (UV) {
+      h.u = c.u;
+      h.v = c.v;
+    }
   }
   return false;
 }
@@ -619,18 +623,18 @@ __device__ __forceinline__ void walk_enter(Walk& w, int32_t c) {
 // which pays one memory latency per leaf instead of one per primitive
 // (caustic scene: 1,067 -> 1,214 Msamples/s, identical images; the exact
 // walk with whole-leaf steps ran at 645 against 895 Mrays/s).
-template <bool EXACT>
+template <bool EXACT, bool UV = true>
 __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack& st, uint32_t& fallbacks) {
   if (w.ref == kWalkLeaf) {
     if constexpr (EXACT) {
-      if (test_prim<EXACT>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
+      if (test_prim<EXACT, UV>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
         w.ref = kWalkDone;
         return;
       }
       if (++w.cur == w.end) w.ref = kWalkPop;
     } else {
       for (; w.cur < w.end; w.cur++)
-        if (test_prim<EXACT>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
+        if (test_prim<EXACT, UV>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
           w.ref = kWalkDone;
           return;
         }
@@ -711,7 +715,7 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
 // size is a multiple of 32).
 // `s` is the scene the lane walks: a fixed scene, or (queries of many scenes)
 // a per-lane copy that begin() replaces with the new query's scene.
-template <bool EXACT, int REFILL, bool PHASED, class Scene, class Begin, class Finish>
+template <bool EXACT, int REFILL, bool PHASED, bool UV = true, class Scene, class Begin, class Finish>
 __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uint32_t total, Begin begin,
                                                 Finish finish, uint32_t& fallbacks) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -746,14 +750,14 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
       }
     }
     if (__all_sync(0xffffffffu, idx < 0) && drained) break;
-    if (w.ref != kWalkDone) walk_step<EXACT>(s, w, st, fallbacks);
+    if (w.ref != kWalkDone) walk_step<EXACT, UV>(s, w, st, fallbacks);
     bool go = w.ref != kWalkDone;
     if (PHASED) {
       const uint32_t leaf = __ballot_sync(0xffffffffu, w.ref == kWalkLeaf);
       const uint32_t inner = __ballot_sync(0xffffffffu, w.ref >= 0);
       go = go && (w.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
     }
-    if (go) walk_step<EXACT>(s, w, st, fallbacks);
+    if (go) walk_step<EXACT, UV>(s, w, st, fallbacks);
     if (!EXACT) {  // the integrator's walk takes a third step, gated the same way
       bool go3 = w.ref != kWalkDone;
       if (PHASED) {
@@ -761,7 +765,7 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
         const uint32_t inner = __ballot_sync(0xffffffffu, w.ref >= 0);
         go3 = go3 && (w.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
       }
-      if (go3) walk_step<EXACT>(s, w, st, fallbacks);
+      if (go3) walk_step<EXACT, UV>(s, w, st, fallbacks);
     }
   }
 }
