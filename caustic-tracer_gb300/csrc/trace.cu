@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
       ctk::Walk& w = f.w;
       load(i, w.r);
       ctk::walk_begin(s, w, ANY);
-      while (w.ref != ctk::kWalkDone) ctk::walk_step<true, BARY && !ANY>(s, w, f.st, fallbacks);
+      while (w.c.ref != ctk::kWalkDone) ctk::walk_step<true, BARY && !ANY>(s, w, f.st, fallbacks);
       overflow |= w.overflow;
       store(i, w.r, w.h);
     }

@@ -555,10 +555,16 @@ __device__ __forceinline__ float prune_bound(const HitF& h) { return h.t + h.err
 // others pushed farthest first with their entry distances), tests one
 // primitive of the current leaf, or pops the stack past entries beyond the
 // closest hit. Equal-cost steps keep the lanes of a warp in step.
-struct alignas(16) Walk {
-  int32_t ref;  // >= 0 interior record, kLeaf: testing [cur, end), kPop, kDone
+// The walk's counters. A step reads them once and writes them back once
+// (one 16-byte access each where the walk lives in local memory).
+struct alignas(16) WalkCtl {
+  int32_t ref;  // >= 0 interior record, kWalkLeaf: testing [cur, end), kWalkPop, kWalkDone
   uint32_t cur, end;
   int32_t sp;
+};
+
+struct alignas(16) Walk {
+  WalkCtl c;
   RayF r;
   HitF h;
   bool any, overflow;
@@ -580,7 +586,9 @@ struct WalkStack {
 // with only the ray), while the integrator's walk gains with its state
 // apart (caustic scene 1,822 -> 1,914 Msamples/s, 100k soup 499 -> 526).
 // With the ray and the frame 16-byte aligned (the counters first, then the
-// ray's three 16-byte groups) the exact walk runs at 912 against 896.
+// ray's three 16-byte groups) the exact walk runs at 912 against 896; with
+// the counters read and written once per step (WalkCtl) at 1,049 against
+// 968 (and the integrator's walk, caustic scene, at 1,969 against 1,915).
 struct WalkFrame {
   Walk w;
   WalkStack st;
@@ -588,36 +596,33 @@ struct WalkFrame {
 
 constexpr int32_t kWalkPop = INT32_MAX, kWalkDone = INT32_MIN, kWalkLeaf = INT32_MIN + 1;
 
+// Enters child `child` (interior record or ~leafword).
+__device__ __forceinline__ void walk_enter(WalkCtl& c, int32_t child) {
+  if (child >= 0) {
+    c.ref = child;
+  } else {
+    const uint32_t word = (uint32_t)~child;
+    c.cur = word >> 3;
+    c.end = c.cur + (word & 7u);
+    c.ref = c.cur < c.end ? kWalkLeaf : kWalkPop;
+  }
+}
+
 // Starts a walk for w.r (tmin/tmax set, inverse direction computed).
 __device__ __forceinline__ void walk_begin(const SceneDev& s, Walk& w, bool any) {
   w.h = HitF{-1, w.r.tmax, 0.0f, 0.0f, 0.0f};
-  w.sp = 0;
   w.any = any;
   w.overflow = false;
-  w.ref = (s.node_count == 0 || box_entry(w.r, s.root_lo[0], s.root_hi[0], s.root_lo[1], s.root_hi[1],
-                                          s.root_lo[2], s.root_hi[2], w.r.tmax) == INFINITY)
-              ? kWalkDone : s.root_ref;
-  if (w.ref < 0 && w.ref != kWalkDone) {  // the root is a leaf
-    const uint32_t word = (uint32_t)~w.ref;
-    w.cur = word >> 3;
-    w.end = w.cur + (word & 7u);
-    w.ref = w.cur < w.end ? kWalkLeaf : kWalkDone;
+  WalkCtl c{kWalkDone, 0u, 0u, 0};
+  if (s.node_count != 0 && box_entry(w.r, s.root_lo[0], s.root_hi[0], s.root_lo[1], s.root_hi[1], s.root_lo[2],
+                                     s.root_hi[2], w.r.tmax) != INFINITY) {
+    walk_enter(c, s.root_ref);  // the root may be a leaf
+    if (c.ref == kWalkPop) c.ref = kWalkDone;
   }
+  w.c = c;
 }
 
-// Enters child `c` (interior record or ~leafword).
-__device__ __forceinline__ void walk_enter(Walk& w, int32_t c) {
-  if (c >= 0) {
-    w.ref = c;
-  } else {
-    const uint32_t word = (uint32_t)~c;
-    w.cur = word >> 3;
-    w.end = w.cur + (word & 7u);
-    w.ref = w.cur < w.end ? kWalkLeaf : kWalkPop;
-  }
-}
-
-// One step; w.ref == kWalkDone when the query is answered. A step of the
+// One step; w.c.ref == kWalkDone when the query is answered. A step of the
 // exact walk tests one primitive of a leaf; a step of the integrator's walk
 // (plain float32 tests, a third of the instructions) tests the whole leaf,
 // which pays one memory latency per leaf instead of one per primitive
@@ -625,23 +630,20 @@ __device__ __forceinline__ void walk_enter(Walk& w, int32_t c) {
 // walk with whole-leaf steps ran at 645 against 895 Mrays/s).
 template <bool EXACT, bool UV = true>
 __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack& st, uint32_t& fallbacks) {
-  if (w.ref == kWalkLeaf) {
+  WalkCtl c = w.c;
+  if (c.ref == kWalkLeaf) {
     if constexpr (EXACT) {
-      if (test_prim<EXACT, UV>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
-        w.ref = kWalkDone;
-        return;
-      }
-      if (++w.cur == w.end) w.ref = kWalkPop;
+      if (test_prim<EXACT, UV>(s, w.r, c.cur, w.h, w.any, fallbacks))
+        c.ref = kWalkDone;
+      else if (++c.cur == c.end)
+        c.ref = kWalkPop;
     } else {
-      for (; w.cur < w.end; w.cur++)
-        if (test_prim<EXACT, UV>(s, w.r, w.cur, w.h, w.any, fallbacks)) {
-          w.ref = kWalkDone;
-          return;
-        }
-      w.ref = kWalkPop;
+      bool found = false;
+      for (; c.cur < c.end && !found; c.cur++) found = test_prim<EXACT, UV>(s, w.r, c.cur, w.h, w.any, fallbacks);
+      c.ref = found ? kWalkDone : kWalkPop;
     }
-  } else if (w.ref >= 0 && w.ref != kWalkPop) {
-    const uint4* q = s.quads + (size_t)w.ref * 4;
+  } else if (c.ref >= 0 && c.ref != kWalkPop) {
+    const uint4* q = s.quads + (size_t)c.ref * 4;
     const uint4 bx = __ldg(q), by = __ldg(q + 1), bz = __ldg(q + 2);
     const int4 c4 = __ldg(reinterpret_cast<const int4*>(q + 3));
     auto f2 = [](uint32_t h) { return __half22float2(*reinterpret_cast<const __half2*>(&h)); };
@@ -659,8 +661,8 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
       if (tb < ta) {
         const float t = ta;
         ta = tb, tb = t;
-        const int32_t c = ca;
-        ca = cb, cb = c;
+        const int32_t k = ca;
+        ca = cb, cb = k;
       }
     };
     order(t0, c0, t1, c1);
@@ -670,30 +672,30 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
     order(t1, c1, t2, c2);
     const int hits = (t0 != INFINITY) + (t1 != INFINITY) + (t2 != INFINITY) + (t3 != INFINITY);
     if (hits == 0) {
-      w.ref = kWalkPop;
-    } else if (w.sp + hits - 1 > kStackSize) {
+      c.ref = kWalkPop;
+    } else if (c.sp + hits - 1 > kStackSize) {
       w.overflow = true;
-      w.ref = kWalkDone;
-      return;
+      c.ref = kWalkDone;
     } else {
-      if (hits > 3) st.e[w.sp++] = make_int2(c3, __float_as_int(t3));
-      if (hits > 2) st.e[w.sp++] = make_int2(c2, __float_as_int(t2));
-      if (hits > 1) st.e[w.sp++] = make_int2(c1, __float_as_int(t1));
-      walk_enter(w, c0);
+      if (hits > 3) st.e[c.sp++] = make_int2(c3, __float_as_int(t3));
+      if (hits > 2) st.e[c.sp++] = make_int2(c2, __float_as_int(t2));
+      if (hits > 1) st.e[c.sp++] = make_int2(c1, __float_as_int(t1));
+      walk_enter(c, c0);
     }
   }
-  if (w.ref == kWalkPop) {
-    w.ref = kWalkDone;
+  if (c.ref == kWalkPop) {
+    c.ref = kWalkDone;
     const float bound = prune_bound(w.h);
-    while (w.sp > 0) {
-      --w.sp;
-      const int2 e = st.e[w.sp];
+    while (c.sp > 0) {
+      --c.sp;
+      const int2 e = st.e[c.sp];
       if (__int_as_float(e.y) <= bound) {
-        walk_enter(w, e.x);
+        walk_enter(c, e.x);
         break;
       }
     }
   }
+  w.c = c;
 }
 
 // Persistent warp loop over `total` queries numbered 0..total-1, handed out in
@@ -725,11 +727,11 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
   WalkStack apart_stack;
   Walk& w = EXACT ? frame.w : apart;
   WalkStack& st = EXACT ? frame.st : apart_stack;
-  w.ref = kWalkDone;
+  w.c.ref = kWalkDone;
   int64_t idx = -1;  // query held by this lane
   bool drained = false;
   for (;;) {
-    const bool idle = w.ref == kWalkDone;
+    const bool idle = w.c.ref == kWalkDone;
     if (idle && idx >= 0) {
       finish((uint32_t)idx, w);
       idx = -1;
@@ -750,20 +752,20 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
       }
     }
     if (__all_sync(0xffffffffu, idx < 0) && drained) break;
-    if (w.ref != kWalkDone) walk_step<EXACT, UV>(s, w, st, fallbacks);
-    bool go = w.ref != kWalkDone;
+    if (w.c.ref != kWalkDone) walk_step<EXACT, UV>(s, w, st, fallbacks);
+    bool go = w.c.ref != kWalkDone;
     if (PHASED) {
-      const uint32_t leaf = __ballot_sync(0xffffffffu, w.ref == kWalkLeaf);
-      const uint32_t inner = __ballot_sync(0xffffffffu, w.ref >= 0);
-      go = go && (w.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
+      const uint32_t leaf = __ballot_sync(0xffffffffu, w.c.ref == kWalkLeaf);
+      const uint32_t inner = __ballot_sync(0xffffffffu, w.c.ref >= 0);
+      go = go && (w.c.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
     }
     if (go) walk_step<EXACT, UV>(s, w, st, fallbacks);
     if (!EXACT) {  // the integrator's walk takes a third step, gated the same way
-      bool go3 = w.ref != kWalkDone;
+      bool go3 = w.c.ref != kWalkDone;
       if (PHASED) {
-        const uint32_t leaf = __ballot_sync(0xffffffffu, w.ref == kWalkLeaf);
-        const uint32_t inner = __ballot_sync(0xffffffffu, w.ref >= 0);
-        go3 = go3 && (w.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
+        const uint32_t leaf = __ballot_sync(0xffffffffu, w.c.ref == kWalkLeaf);
+        const uint32_t inner = __ballot_sync(0xffffffffu, w.c.ref >= 0);
+        go3 = go3 && (w.c.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
       }
       if (go3) walk_step<EXACT, UV>(s, w, st, fallbacks);
     }

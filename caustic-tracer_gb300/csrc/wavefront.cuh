@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
           ctk::walk_stackless<false>(sc, w.r, w.h, i >= n_ext, fallbacks);
       } else {
         ctk::walk_begin(sc, w, i >= n_ext);
-        while (w.ref != ctk::kWalkDone) ctk::walk_step<false>(sc, w, st, fallbacks);
+        while (w.c.ref != ctk::kWalkDone) ctk::walk_step<false>(sc, w, st, fallbacks);
       }
       finish(i, w);
     }
