@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
     }
   };
   if (VARIANT == 0) {
-    ctk::walk_persistent<true, 6, false, BARY && !ANY>(
+    ctk::walk_persistent<true, 6, false, BARY && !ANY, ANY ? 1 : 0>(
         s, queue, n,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
       ctk::Walk& w = f.w;
       load(i, w.r);
       ctk::walk_begin(s, w, ANY);
-      while (w.c.ref != ctk::kWalkDone) ctk::walk_step<true, BARY && !ANY>(s, w, f.st, fallbacks);
+      while (w.c.ref != ctk::kWalkDone) ctk::walk_step<true, BARY && !ANY, ANY ? 1 : 0>(s, w, f.st, fallbacks);
       overflow |= w.overflow;
       store(i, w.r, w.h);
     }

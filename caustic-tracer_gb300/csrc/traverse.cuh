@@ -628,18 +628,22 @@ __device__ __forceinline__ void walk_begin(const SceneDev& s, Walk& w, bool any)
 // which pays one memory latency per leaf instead of one per primitive
 // (caustic scene: 1,067 -> 1,214 Msamples/s, identical images; the exact
 // walk with whole-leaf steps ran at 645 against 895 Mrays/s).
-template <bool EXACT, bool UV = true>
+// ANYQ: the query kind when the kernel fixes it (0 closest, 1 any hit), so
+// the step does not read it from the walk; -1 reads w.any (queries of both
+// kinds in one launch).
+template <bool EXACT, bool UV = true, int ANYQ = -1>
 __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack& st, uint32_t& fallbacks) {
+  const bool any = ANYQ < 0 ? w.any : ANYQ > 0;
   WalkCtl c = w.c;
   if (c.ref == kWalkLeaf) {
     if constexpr (EXACT) {
-      if (test_prim<EXACT, UV>(s, w.r, c.cur, w.h, w.any, fallbacks))
+      if (test_prim<EXACT, UV>(s, w.r, c.cur, w.h, any, fallbacks))
         c.ref = kWalkDone;
       else if (++c.cur == c.end)
         c.ref = kWalkPop;
     } else {
       bool found = false;
-      for (; c.cur < c.end && !found; c.cur++) found = test_prim<EXACT, UV>(s, w.r, c.cur, w.h, w.any, fallbacks);
+      for (; c.cur < c.end && !found; c.cur++) found = test_prim<EXACT, UV>(s, w.r, c.cur, w.h, any, fallbacks);
       c.ref = found ? kWalkDone : kWalkPop;
     }
   } else if (c.ref >= 0 && c.ref != kWalkPop) {
@@ -717,7 +721,7 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
 // size is a multiple of 32).
 // `s` is the scene the lane walks: a fixed scene, or (queries of many scenes)
 // a per-lane copy that begin() replaces with the new query's scene.
-template <bool EXACT, int REFILL, bool PHASED, bool UV = true, class Scene, class Begin, class Finish>
+template <bool EXACT, int REFILL, bool PHASED, bool UV = true, int ANYQ = -1, class Scene, class Begin, class Finish>
 __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uint32_t total, Begin begin,
                                                 Finish finish, uint32_t& fallbacks) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -752,14 +756,14 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
       }
     }
     if (__all_sync(0xffffffffu, idx < 0) && drained) break;
-    if (w.c.ref != kWalkDone) walk_step<EXACT, UV>(s, w, st, fallbacks);
+    if (w.c.ref != kWalkDone) walk_step<EXACT, UV, ANYQ>(s, w, st, fallbacks);
     bool go = w.c.ref != kWalkDone;
     if (PHASED) {
       const uint32_t leaf = __ballot_sync(0xffffffffu, w.c.ref == kWalkLeaf);
       const uint32_t inner = __ballot_sync(0xffffffffu, w.c.ref >= 0);
       go = go && (w.c.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
     }
-    if (go) walk_step<EXACT, UV>(s, w, st, fallbacks);
+    if (go) walk_step<EXACT, UV, ANYQ>(s, w, st, fallbacks);
     if (!EXACT) {  // the integrator's walk takes a third step, gated the same way
       bool go3 = w.c.ref != kWalkDone;
       if (PHASED) {
@@ -767,7 +771,7 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
         const uint32_t inner = __ballot_sync(0xffffffffu, w.c.ref >= 0);
         go3 = go3 && (w.c.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
       }
-      if (go3) walk_step<EXACT, UV>(s, w, st, fallbacks);
+      if (go3) walk_step<EXACT, UV, ANYQ>(s, w, st, fallbacks);
     }
   }
 }
