@@ -706,9 +706,10 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
 // warp-sized batches from *counter. begin(i, w) loads query i into w.r and
 // calls walk_begin; finish(i, w) consumes the answer. Lanes whose queries are
 // answered are refilled as soon as REFILL lanes of the warp are idle, so
-// lanes keep stepping instead of waiting for the warp's slowest ray (6 suits
-// the exact query walk, 0.7 % ahead of 8; 12 the integrator's, 1.7 % ahead
-// of 16 on the batched soups and 0.5 % behind it on the caustic scene). Each round of the
+// lanes keep stepping instead of waiting for the warp's slowest ray (5 suits
+// the exact query walk: 1,072 Mrays/s against 1,065-1,069 at 3, 4 or 6 and
+// 1,061 at 8; 12 the integrator's, 1.7 % ahead of 16 on the batched soups
+// and 0.5 % behind it on the caustic scene). Each round of the
 // exact walk takes two steps per lane, which halves the refill bookkeeping
 // (one step per round ran 5 % slower on the 1M-triangle query walk, three or
 // four 20-35 % slower); the integrator's walk, whose steps test whole leaves,
@@ -721,6 +722,11 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
 // size is a multiple of 32).
 // `s` is the scene the lane walks: a fixed scene, or (queries of many scenes)
 // a per-lane copy that begin() replaces with the new query's scene.
+// Query numbers are below 2^32 - 1 (`total` is a uint32_t), so all ones marks
+// a lane without a query (one register instead of a signed 64-bit index:
+// exact 1M-soup walk 1,070 against 1,063 Mrays/s).
+constexpr uint32_t kNoQuery = 0xffffffffu;
+
 template <bool EXACT, int REFILL, bool PHASED, bool UV = true, int ANYQ = -1, class Scene, class Begin, class Finish>
 __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uint32_t total, Begin begin,
                                                 Finish finish, uint32_t& fallbacks) {
@@ -732,13 +738,13 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
   Walk& w = EXACT ? frame.w : apart;
   WalkStack& st = EXACT ? frame.st : apart_stack;
   w.c.ref = kWalkDone;
-  int64_t idx = -1;  // query held by this lane
+  uint32_t idx = kNoQuery;  // query held by this lane
   bool drained = false;
   for (;;) {
     const bool idle = w.c.ref == kWalkDone;
-    if (idle && idx >= 0) {
-      finish((uint32_t)idx, w);
-      idx = -1;
+    if (idle && idx != kNoQuery) {
+      finish(idx, w);
+      idx = kNoQuery;
     }
     const uint32_t want = __ballot_sync(0xffffffffu, idle);
     if (!drained && (__popc(want) >= REFILL || want == 0xffffffffu)) {
@@ -755,7 +761,7 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
         }
       }
     }
-    if (__all_sync(0xffffffffu, idx < 0) && drained) break;
+    if (__all_sync(0xffffffffu, idx == kNoQuery) && drained) break;
     if (w.c.ref != kWalkDone) walk_step<EXACT, UV, ANYQ>(s, w, st, fallbacks);
     bool go = w.c.ref != kWalkDone;
     if (PHASED) {
