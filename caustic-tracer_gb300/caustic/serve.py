@@ -93,7 +93,7 @@ class Executor(Protocol):
 
 
 class RenderServer:
-    POLICIES = ("round_robin", "fifo")
+    POLICIES = ("round_robin", "fifo", "srpt")
 
     def __init__(self, executor: Executor, budget_bytes: int = 120 << 30, step_paths: int = 16 << 20,
                  min_chunk_paths: int = 16 << 20, max_passes_per_step: Optional[int] = None,
@@ -185,9 +185,11 @@ class RenderServer:
         """One step: requests with passes left, all of the first one's walk
         class, packed into at most step_paths paths (one wave). Order: round
         robin from where the last step stopped (small requests finish within a
-        few steps of arriving; large ones share the GPU), or fifo: always from
+        few steps of arriving; large ones share the GPU), fifo: always from
         the oldest (a large request runs as fast as alone, later ones only fill
-        what is left of each wave). Each request gets an equal share of the
+        what is left of each wave), or srpt: the fewest samples left first
+        (small requests go ahead of large ones, and a large request is not
+        spread over the steps of many others; ties by admission order). Each request gets an equal share of the
         step, but at least min_chunk_paths (a request's chunk keeps its scene
         hot in L2 for a while) and at least one pass, at most what it still
         needs and what still fits; requests that do not fit wait for the next
@@ -199,6 +201,8 @@ class RenderServer:
         if self.policy == "round_robin":
             k = next((i for i, a in enumerate(pending) if a.seq >= self._next), 0)
             pending = pending[k:] + pending[:k]
+        elif self.policy == "srpt":
+            pending.sort(key=lambda a: ((a.req.spp - a.issued) * a.req.pixels, a.seq))
         cls = self.ex.walk_class(pending[0].req.scene)
         share = max(self.step_paths / len(pending), min(self.min_chunk, self.step_paths))
         room = self.step_paths

@@ -227,3 +227,22 @@ def test_fifo_policy_runs_the_oldest_request_at_full_rate():
     assert len(steps_with_0) == 3 and all(dict((r, p) for r, _, p in s)[0] == 4 for s in steps_with_0)
     with pytest.raises(ValueError):
         RenderServer(ex, policy="lifo")
+
+
+def test_srpt_policy_runs_the_request_with_least_work_left_first():
+    ex = FakeExecutor({"a": 0})
+    step_paths = 64 * 64 * 4
+    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=step_paths, clock=Clock(), policy="srpt")
+    srv.submit(_req(0, 64, 12))   # large, admitted first
+    srv.submit(_req(1, 32, 8))    # two steps' worth of a quarter wave each
+    srv.submit(_req(2, 16, 4))    # smallest
+    results = srv.drain()
+    order = [r.request.rid for r in results]
+    assert order == [2, 1, 0]
+    first = dict((r, p) for r, _, p in ex.steps[0])
+    assert first[2] == 4 and first[1] == 8  # the small ones take all they need first
+    assert first.get(0, 0) == (step_paths - 16 * 16 * 4 - 32 * 32 * 8) // (64 * 64)
+    for r in results:  # every request still gets exactly its passes, in order
+        assert [f for f, _ in r.image] == sorted(f for f, _ in r.image)
+        assert sum(p for _, p in r.image) == r.request.spp
+
