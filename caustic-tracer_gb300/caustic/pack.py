@@ -57,10 +57,12 @@ class PackedScene:
 
     @property
     def device_bytes_estimate(self) -> int:
-        """Device bytes of the uploaded scene (arrays + 64 B per interior node)."""
+        """Device bytes of the uploaded scene: the packed arrays, 64 B per
+        interior node (4-wide records) and 96 B per primitive (plane records
+        and the compact copy the exact tests read)."""
         interior = max(1, (self.node_count - 1) // 2)
         return (self.prims.nbytes + self.nodes.nbytes + self.mats.nbytes + self.lights.nbytes
-                + self.prim_object.nbytes + 64 * interior)
+                + self.prim_object.nbytes + 64 * interior + 96 * self.prim_count)
 
 
 def sky_struct(sky: Sky) -> _abi.ct_sky:

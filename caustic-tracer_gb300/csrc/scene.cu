@@ -381,6 +381,16 @@ ct_status validate_view(const ct_packed_scene_view& v) {
   return CT_OK;
 }
 
+// tris[3p + k] = prims[4p + k], k < 3: the vertices (or a sphere's centre and
+// radius) of each primitive without its fourth record, for the exact tests.
+__global__ void k_compact_prims(const float4* __restrict__ prims, uint32_t n, float4* __restrict__ tris) {
+  const size_t total = (size_t)n * 3, stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += stride) {
+    const size_t p = i / 3;
+    tris[i] = __ldg(prims + p * 4 + (i - p * 3));
+  }
+}
+
 // The scene's arrays share one allocation from the per-device stream-ordered
 // pool (scene create and destroy then cost no cudaMalloc / cudaFree, and the
 // latter would wait for the whole device).
@@ -398,6 +408,14 @@ ct_status upload(ct_scene* s, DeviceBuffer& b, char*& cursor, const T* src, size
   return CT_OK;
 }
 
+// A slot of the arena that a kernel fills (no host copy).
+ct_status carve(ct_scene*, DeviceBuffer& b, char*& cursor, size_t bytes) {
+  b.ptr = cursor;
+  b.bytes = bytes;
+  cursor += arena_slot(bytes);
+  return CT_OK;
+}
+
 void destroy(ct_scene* s) {
   if (!s) return;
   int prev = 0;
@@ -405,7 +423,7 @@ void destroy(ct_scene* s) {
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (DeviceBuffer* b : {&s->prims, &s->nodes, &s->quads, &s->mats, &s->lights, &s->prim_object, &s->planes,
-                          &s->counters})
+                          &s->tris, &s->counters})
     b->ptr = nullptr, b->bytes = 0;  // slices of the arena
   if (s->arena) path_free(s->arena, s->stream);
   s->io.release(&s->device_bytes, s->stream);
@@ -553,6 +571,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
                        arena_slot(std::max<size_t>(v.light_count, 1) * sizeof(int32_t)) +
                        arena_slot(std::max<size_t>(v.prim_count, 1) * sizeof(uint32_t)) +
                        arena_slot(std::max<size_t>(planes.size(), 3) * sizeof(float4)) +
+                       arena_slot(std::max<size_t>((size_t)v.prim_count * 3, 3) * sizeof(float4)) +
                        arena_slot(kCounterWords * sizeof(uint32_t));
   if ((st = path_alloc(s->device, arena, s->stream, &s->arena)) != CT_OK) return bail(st);
   s->device_bytes += arena;
@@ -564,8 +583,19 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
       (st = upload(s, s->lights, cursor, v.lights, v.light_count, 1)) != CT_OK ||
       (st = upload(s, s->prim_object, cursor, v.prim_object, v.prim_count, 1)) != CT_OK ||
       (st = upload(s, s->planes, cursor, planes.data(), planes.size(), 3)) != CT_OK ||
+      (st = carve(s, s->tris, cursor, std::max<size_t>((size_t)v.prim_count * 3, 3) * sizeof(float4))) != CT_OK ||
       (st = upload(s, s->counters, cursor, (const uint32_t*)nullptr, 0, kCounterWords)) != CT_OK)
     return bail(st);
+  if (v.prim_count) {
+    const size_t total = (size_t)v.prim_count * 3;
+    const unsigned blocks = (unsigned)std::min<size_t>((total + 255) / 256, 4096);
+    k_compact_prims<<<blocks, 256, 0, s->stream>>>(s->prims.as<float4>(), v.prim_count, s->tris.as<float4>());
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "k_compact_prims: %s", cudaGetErrorString(err)));
+  } else {
+    cudaError_t err = cudaMemsetAsync(s->tris.ptr, 0, s->tris.bytes, s->stream);
+    if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "scene upload: %s", cudaGetErrorString(err)));
+  }
   if (v.mat_count == 0 && v.mats != nullptr) {
     // The reference always allocates one material record (pack.ts:122).
     cudaError_t err = cudaMemcpyAsync(s->mats.ptr, v.mats, CT_MAT_STRIDE * sizeof(float), cudaMemcpyHostToDevice, s->stream);
@@ -581,6 +611,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   d.nodes = s->nodes.as<float4>();
   d.quads = s->quads.as<uint4>();
   d.planes = s->planes.as<float4>();
+  d.tris = s->tris.as<float4>();
   d.mats = s->mats.as<float4>();
   d.lights = s->lights.as<int32_t>();
   d.prim_object = s->prim_object.as<uint32_t>();

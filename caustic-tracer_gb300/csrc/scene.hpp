@@ -61,6 +61,7 @@ struct ct_scene {
   void* arena = nullptr;
   ct::DeviceBuffer prims, nodes, quads, mats, lights, prim_object;
   ct::DeviceBuffer planes;  // 3 float4 plane records per primitive (integrator tests)
+  ct::DeviceBuffer tris;    // 3 float4 per primitive: a, b, c of prims (exact tests), built on the device
   uint32_t prim_count = 0, node_count = 0, interior_count = 0, mat_count = 0, light_count = 0;
   uint32_t depth = 0;       // deepest root-to-leaf path, in nodes
   uint32_t stack_need = 0;  // deepest stack the ordered walk can build
