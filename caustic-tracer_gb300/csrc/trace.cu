@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(128, 12) k_trace(ctk::SceneDev s, const float4
     }
   };
   if (VARIANT == 0) {
-    ctk::walk_persistent<true, 5, false, BARY && !ANY, ANY ? 1 : 0>(
+    ctk::walk_persistent<true, 5, false, 2, BARY && !ANY, ANY ? 1 : 0>(
         s, queue, n,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);

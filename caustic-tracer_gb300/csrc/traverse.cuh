@@ -713,12 +713,12 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
 // lanes keep stepping instead of waiting for the warp's slowest ray (5 suits
 // the exact query walk: 1,072 Mrays/s against 1,065-1,069 at 3, 4 or 6 and
 // 1,061 at 8; 12 the integrator's, 1.7 % ahead of 16 on the batched soups
-// and 0.5 % behind it on the caustic scene). Each round of the
-// exact walk takes two steps per lane, which halves the refill bookkeeping
-// (one step per round ran 5 % slower on the 1M-triangle query walk, three or
-// four 20-35 % slower); the integrator's walk, whose steps test whole leaves,
-// takes three (batched soups +2.3 %, a 100k soup +1.5 %, the caustic scene
-// unchanged; one step per round: 8 % slower). With PHASED, the steps after
+// and 0.5 % behind it on the caustic scene). Each round takes STEPS walk
+// steps per lane: the exact walk two (one step per round ran 5 % slower on
+// the 1M-triangle query walk, three 20 % slower), the integrator's walk,
+// whose steps test whole leaves and whose later steps are gated by majority,
+// 8 for one scene and 12 for a batch (their callers give the measurements).
+// With PHASED, the steps after
 // the first move either the lanes testing primitives or those expanding
 // records, whichever are more, so each branch runs with fuller warps; every lane still makes its own tests in the same
 // order (measured: 1.5 % faster for the integrator's walk, 4 % slower for the
@@ -731,7 +731,8 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
 // exact 1M-soup walk 1,070 against 1,063 Mrays/s).
 constexpr uint32_t kNoQuery = 0xffffffffu;
 
-template <bool EXACT, int REFILL, bool PHASED, bool UV = true, int ANYQ = -1, class Scene, class Begin, class Finish>
+template <bool EXACT, int REFILL, bool PHASED, int STEPS, bool UV = true, int ANYQ = -1, class Scene, class Begin,
+          class Finish>
 __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uint32_t total, Begin begin,
                                                 Finish finish, uint32_t& fallbacks) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -769,9 +770,8 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
     // One copy of the step in the loop body (not unrolled): the integrator's
     // walk runs 1 % faster on the caustic scene, the exact walk unchanged
     // with half the spill slots.
-    constexpr int kSteps = EXACT ? 2 : 3;
 #pragma unroll 1
-    for (int k = 0; k < kSteps; k++) {
+    for (int k = 0; k < STEPS; k++) {
       bool go = w.c.ref != kWalkDone;
       if (PHASED && k > 0) {  // steps after the first move the majority kind
         const uint32_t leaf = __ballot_sync(0xffffffffu, w.c.ref == kWalkLeaf);

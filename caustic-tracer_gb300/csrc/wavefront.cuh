@@ -229,14 +229,16 @@ enum WalkForm : int { kWalkThread = 0, kWalkPersistent = 1, kWalkSkip = 2, kWalk
 
 // Closest hits of the bounce-b path queue plus the shadow rays of bounce b-1.
 // Blocks of 128 per SM, measured per walk form: the ordered walk per thread
-// at 16 (32 registers), the persistent ordered walk at 12 (40 registers:
-// its refill state spills at 32; 925 vs 902 Msamples/s on the caustic
-// scene), the skip-link walk at 8 (it keeps its registers).
-template <int FORM>
-constexpr int trace_min_blocks() { return FORM == 2 ? 8 : FORM == 1 ? 12 : 16; }
+// at 16 (32 registers), the persistent ordered walk of one scene at 10 (48
+// registers, no spills: caustic scene 2,020 against 1,986 Msamples/s at 12
+// blocks and 1,894 at 16, the 100k soup 567 against 544) and of a batch at
+// 12 (40 registers; batched soups 1,335 against 1,320 at 10), the skip-link
+// walk at 8 (it keeps its registers).
+template <int FORM, bool BATCH>
+constexpr int trace_min_blocks() { return FORM == 2 ? 8 : FORM == 1 ? (BATCH ? 12 : 10) : 16; }
 
 template <int FORM, bool BATCH>
-__global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(WaveArgs a, int32_t bounce) {
+__global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM, BATCH>()) k_trace(WaveArgs a, int32_t bounce) {
   const uint32_t n_ext = bounce <= a.max_bounces ? a.counts[bounce] : 0u;
   const uint32_t n_sh = bounce > 0 ? a.counts[a.max_bounces + 2 + bounce - 1] : 0u;
   uint32_t fallbacks = 0;
@@ -273,8 +275,12 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
   // A batch query copies its job's scene record into registers once, so the
   // walk reads the base pointers as often as the single-scene kernel reads
   // its kernel parameters.
+  // Walk steps per refill round (measured): one scene 8 (caustic scene 2,082
+  // Msamples/s against 2,021 at 3, 2,085 at 6 and 2,020 at 12; 100k soup 591
+  // against 567 at 3 and 595 at 12), a batch of soups 12 (1,406 against 1,334
+  // at 3 and 1,398 at 8).
   if constexpr (FORM == kWalkPersistent && !BATCH) {
-    ctk::walk_persistent<false, 12, true>(
+    ctk::walk_persistent<false, 12, true, 8>(
         a.scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);
@@ -283,7 +289,7 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM>()) k_trace(Wave
         finish, fallbacks);
   } else if constexpr (FORM == kWalkPersistent) {
     ctk::SceneDev lane_scene = a.jobs[0].scene;
-    ctk::walk_persistent<false, 12, true>(
+    ctk::walk_persistent<false, 12, true, 12>(
         lane_scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);
