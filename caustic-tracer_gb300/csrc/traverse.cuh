@@ -712,8 +712,7 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
 // answered are refilled as soon as REFILL lanes of the warp are idle, so
 // lanes keep stepping instead of waiting for the warp's slowest ray (5 suits
 // the exact query walk: 1,072 Mrays/s against 1,065-1,069 at 3, 4 or 6 and
-// 1,061 at 8; 12 the integrator's, 1.7 % ahead of 16 on the batched soups
-// and 0.5 % behind it on the caustic scene). Each round takes STEPS walk
+// 1,061 at 8; 6 the integrator's, whose callers give the measurements). Each round takes STEPS walk
 // steps per lane: the exact walk two (one step per round ran 5 % slower on
 // the 1M-triangle query walk, three 20 % slower), the integrator's walk,
 // whose steps test whole leaves and whose later steps are gated by majority,

@@ -278,9 +278,11 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM, BATCH>()) k_tra
   // Walk steps per refill round (measured): one scene 8 (caustic scene 2,082
   // Msamples/s against 2,021 at 3, 2,085 at 6 and 2,020 at 12; 100k soup 591
   // against 567 at 3 and 595 at 12), a batch of soups 12 (1,406 against 1,334
-  // at 3 and 1,398 at 8).
+  // at 3 and 1,398 at 8; 1,425 at 16). Refill at 6 idle lanes: caustic
+  // 2,092, soup 603, batched 1,436 against 2,092 / 599 / 1,428 at 8, 2,079 /
+  // 591 / 1,404 at 12 and 2,059 / 577 / 1,370 at 16 (4 as 6 within 0.3 %).
   if constexpr (FORM == kWalkPersistent && !BATCH) {
-    ctk::walk_persistent<false, 12, true, 8>(
+    ctk::walk_persistent<false, 6, true, 8>(
         a.scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);
@@ -289,7 +291,7 @@ __global__ void __launch_bounds__(kBlock, trace_min_blocks<FORM, BATCH>()) k_tra
         finish, fallbacks);
   } else if constexpr (FORM == kWalkPersistent) {
     ctk::SceneDev lane_scene = a.jobs[0].scene;
-    ctk::walk_persistent<false, 12, true, 12>(
+    ctk::walk_persistent<false, 6, true, 12>(
         lane_scene, a.counts + 2 * a.max_bounces + 8 + bounce, n_ext + n_sh,
         [&](uint32_t i, ctk::Walk& w) {
           load(i, w.r);
