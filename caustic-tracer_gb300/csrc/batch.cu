@@ -69,9 +69,11 @@ namespace {
 // Paths per wave and path-state sets (streams) of a batch of several waves:
 // on the 256-scene workload 8 Mi paths and one set 952 Msamples/s, two sets
 // 1,075, four 1,137; 24 Mi paths and four sets 1,201 (six: 1,202); 32 Mi
-// and four sets 1,207 (48 Mi: 1,216). Four sets of 32 Mi paths hold 22 GB of
-// path state; a batch takes only what its largest wave needs.
-constexpr uint64_t kDefaultWavePaths = 32ull << 20;
+// and four sets 1,207 (48 Mi: 1,216). With the faster walk of today: 24,
+// 32, 40, 48, 64 Mi and four sets 1,428 / 1,436 / 1,439 / 1,449 / 1,446;
+// 48 Mi and six sets 1,441. Four sets of 48 Mi paths hold 33 GB of path
+// state; a batch takes only what its largest wave needs.
+constexpr uint64_t kDefaultWavePaths = 48ull << 20;
 constexpr int kWaveSets = 4;
 
 // Trace walk of job j's waves: the batch's walk, or (kWalkPerJob) the one its

@@ -201,7 +201,7 @@ void ct_scene_destroy(ct_scene* scene);
  * stream-ordered pool for the duration of the call's work, and the pool
  * keeps its high-water mark for reuse (168 bytes per path in flight: a
  * render of several waves holds up to four sets of 16 Mi paths, 11 GiB; a
- * batch of several waves up to four sets of 32 Mi, 22 GiB).                */
+ * batch of several waves up to four sets of 48 Mi, 33 GiB).                */
 uint64_t ct_scene_device_bytes(const ct_scene* scene);
 
 /* Per-scene tuning knobs, set by callers or an autotuner. No counterpart in
@@ -282,7 +282,7 @@ ct_status ct_render_image_device(ct_scene* scene, const ct_camera_frame* frame,
  * (tracer.ts:361-395) with frame indices first_frame_index + k, adding into
  * the job's device sum buffer `accum` (width*height*3 floats). Results equal
  * those of the single-scene entry points for the same frame indices.
- * The paths of all jobs share waves of up to wave_paths paths (0 = 32 Mi),
+ * The paths of all jobs share waves of up to wave_paths paths (0 = 48 Mi),
  * up to four waves in flight on as many streams, added in pass order;
  * walk selects the trace walk: -1 = each job the walk its scene uses alone
  * (so every result equals its single-scene render bit for bit; a wave holds
