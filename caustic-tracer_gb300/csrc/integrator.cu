@@ -1,7 +1,7 @@
 // Single-scene path integrator: accumulatePass / renderImage (tracer.ts:348-395)
 // on the wavefront kernels of wavefront.cuh.
 //
-// A render of P passes runs in waves of up to kMaxWavePaths paths; a wave
+// A render of P passes runs in waves of whole passes (default_wave_paths); a wave
 // holds whole passes (path id = pass * W*H + pixel) and its accumulate
 // kernel adds each pixel's samples in pass order, so results do not depend
 // on the wave size.
@@ -22,9 +22,23 @@ namespace {
 // streams, so a wave's last bounces overlap the next waves' first ones.
 // Caustic scene, 1080p x 64 spp (Msamples/s): one set of 8 Mi 1,205; three
 // of 8 Mi 1,651; three of 16 Mi 1,787; four of 16 Mi 1,819 (11 GB of path
-// state); four of 24 Mi 1,807; six of 16 Mi 1,805.
-constexpr uint64_t kMaxWavePaths = 16ull << 20;
+// state); four of 24 Mi 1,807; six of 16 Mi 1,805. With the faster walk of
+// today, four sets and waves of 16 / 24 / 32 / 48 / 64 Mi: 2,090 / 2,093 /
+// 2,154 / 2,174 / 2,179 at 64 spp (8 / 6 / 4 / 3 / 2 waves), but at 16 spp
+// (33 M paths) 2,002 with two waves of 16 Mi against 1,926 with one of 48 Mi,
+// and at 32 spp 2,087 (16 Mi) / 2,107 (48 Mi, two waves) / 2,064 (64 Mi,
+// one); at 128 spp 2,095 / 2,167 / 2,198. So a render is split into at least
+// two waves, each of at least 16 Mi and at most 48 Mi paths (four sets of
+// 48 Mi hold 34 GB of path state).
+constexpr uint64_t kMinWavePaths = 16ull << 20;
+constexpr uint64_t kMaxWavePaths = 48ull << 20;
 constexpr int kRenderSets = 4;
+
+// Paths per wave when the scene sets none: half the render, within
+// [kMinWavePaths, kMaxWavePaths] (whole passes are then packed up to it).
+uint64_t default_wave_paths(uint64_t total_paths) {
+  return std::min(kMaxWavePaths, std::max(kMinWavePaths, (total_paths + 1) / 2));
+}
 
 // The scene's side streams and events for renders of several waves.
 ct_status render_streams(ct_scene* s, int sets) {
@@ -63,7 +77,8 @@ bool whole_paths(const ct_scene* s, int form) {
 ct_status run_passes(ct_scene* s, const ct_camera_frame& frame, uint32_t width, uint32_t height, uint32_t first,
                      uint32_t passes, const ct_trace_options& o, float* accum, float* sumsq, cudaStream_t stream) {
   const uint64_t pixels = (uint64_t)width * height;
-  const uint64_t wave_paths = s->opt_wave_paths > 0 ? (uint64_t)s->opt_wave_paths : kMaxWavePaths;
+  const uint64_t wave_paths =
+      s->opt_wave_paths > 0 ? (uint64_t)s->opt_wave_paths : default_wave_paths(pixels * (uint64_t)passes);
   const uint64_t per_wave = std::max<uint64_t>(1, std::min<uint64_t>(passes, wave_paths / pixels));
   const uint64_t cap = per_wave * pixels;
   const int32_t B = o.max_bounces;

@@ -200,8 +200,8 @@ void ct_scene_destroy(ct_scene* scene);
  * render or batch is not part of it: it comes from a per-device
  * stream-ordered pool for the duration of the call's work, and the pool
  * keeps its high-water mark for reuse (168 bytes per path in flight: a
- * render of several waves holds up to four sets of 16 Mi paths, 11 GiB; a
- * batch of several waves up to four sets of 48 Mi, 33 GiB).                */
+ * render of several waves holds up to four sets of 48 Mi paths, 33 GiB, and
+ * so does a batch of several waves).                                     */
 uint64_t ct_scene_device_bytes(const ct_scene* scene);
 
 /* Per-scene tuning knobs, set by callers or an autotuner. No counterpart in
@@ -209,7 +209,8 @@ uint64_t ct_scene_device_bytes(const ct_scene* scene);
  *   CT_OPT_WALK        integrator trace walk: -1 chosen from the tree (default),
  *                      0 ordered walk per thread, 1 ordered walk with persistent
  *                      lane refill, 2 stackless skip-link walk (intersect.ts:290)
- *   CT_OPT_WAVE_PATHS  paths per wave (0 = library default, 16 Mi)
+ *   CT_OPT_WAVE_PATHS  paths per wave (0 = library default: half the render's
+ *                      paths, at least 16 Mi and at most 48 Mi)
  *   CT_OPT_TRACE_BLOCKS  resident 128-thread blocks per SM of the integrator's
  *                      trace (or whole-path) launches of a single-scene render,
  *                      1..64, capped at the kernel's occupancy (0 = as many as
