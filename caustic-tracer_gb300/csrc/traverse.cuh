@@ -712,17 +712,16 @@ __device__ __forceinline__ void walk_step(const SceneDev& s, Walk& w, WalkStack&
 // answered are refilled as soon as REFILL lanes of the warp are idle, so
 // lanes keep stepping instead of waiting for the warp's slowest ray (5 suits
 // the exact query walk: 1,072 Mrays/s against 1,065-1,069 at 3, 4 or 6 and
-// 1,061 at 8; 6 the integrator's, whose callers give the measurements). Each round takes STEPS walk
-// steps per lane: the exact walk two (one step per round ran 5 % slower on
-// the 1M-triangle query walk, three 20 % slower), the integrator's walk,
-// whose steps test whole leaves and whose later steps are gated by majority,
-// 8 for one scene and 12 for a batch (their callers give the measurements).
-// With PHASED, the steps after
-// the first move either the lanes testing primitives or those expanding
-// records, whichever are more, so each branch runs with fuller warps; every lane still makes its own tests in the same
-// order (measured: 1.5 % faster for the integrator's walk, 4 % slower for the
-// exact query walk). All 32 lanes of every warp must call this (the block
-// size is a multiple of 32).
+// 1,061 at 8; 6 the integrator's). Each round takes STEPS walk steps per
+// lane: the exact walk two (one step per round ran 5 % slower on the
+// 1M-triangle query walk, three 20 % slower), the integrator's walk, whose
+// steps test whole leaves, 8 for one scene and 12 for a batch (the callers
+// in wavefront.cuh give the measurements). With PHASED, the steps after the
+// first move either the lanes testing primitives or those expanding records,
+// whichever are more, so each branch runs with fuller warps; every lane
+// still makes its own tests in the same order (the integrator's walk gains,
+// the exact query walk loses 2-4 %). All 32 lanes of every warp must call
+// this (the block size is a multiple of 32).
 // `s` is the scene the lane walks: a fixed scene, or (queries of many scenes)
 // a per-lane copy that begin() replaces with the new query's scene.
 // Query numbers are below 2^32 - 1 (`total` is a uint32_t), so all ones marks
