@@ -295,51 +295,6 @@ std::vector<uint4> half_records(const std::vector<float4>& recs) {
   return out;
 }
 
-// Plane records of the integrator's primitive tests, 48 bytes per primitive
-// (Havel and Herout, "Yet Faster Ray-Triangle Intersection (Using SSE4)",
-// IEEE TVCG 16(3), 2010). For a triangle (a, b, c) with n = (b-a) x (c-a):
-//   [0] n, n.a   [1] n1 = ((c-a) x n) / |n|^2, -n1.a   [2] n2 = (n x (b-a)) / |n|^2, -n2.a
-// so that n1.(p-a) and n2.(p-a) are the barycentric weights of b and c (the
-// reference's u and v) of a point p in the plane. Computed in float64 and
-// rounded once. A degenerate triangle (n = 0) gets zero records, which the
-// test rejects as parallel. A sphere: [0] centre, radius  [1] NaN marker.
-std::vector<float4> plane_records(const ct_packed_scene_view& v) {
-  std::vector<float4> out((size_t)v.prim_count * 3);
-  for (uint32_t p = 0; p < v.prim_count; p++) {
-    const float* q = v.prims + (size_t)p * CT_PRIM_STRIDE;
-    float4* o = &out[(size_t)p * 3];
-    if (q[3] == CT_PRIM_SPHERE) {
-      o[0] = make_float4(q[0], q[1], q[2], q[4]);
-      o[1] = make_float4(NAN, 0.0f, 0.0f, 0.0f);
-      o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      continue;
-    }
-    const double a[3] = {q[0], q[1], q[2]};
-    const double e1[3] = {(double)q[4] - a[0], (double)q[5] - a[1], (double)q[6] - a[2]};
-    const double e2[3] = {(double)q[8] - a[0], (double)q[9] - a[1], (double)q[10] - a[2]};
-    auto cross = [](const double* x, const double* y, double* z) {
-      z[0] = x[1] * y[2] - x[2] * y[1];
-      z[1] = x[2] * y[0] - x[0] * y[2];
-      z[2] = x[0] * y[1] - x[1] * y[0];
-    };
-    auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
-    double n[3], n1[3], n2[3];
-    cross(e1, e2, n);
-    const double l2 = dot(n, n);
-    if (!(l2 > 0.0) || !std::isfinite(l2)) {
-      o[0] = o[1] = o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      continue;
-    }
-    cross(e2, n, n1);
-    cross(n, e1, n2);
-    for (int k = 0; k < 3; k++) n1[k] /= l2, n2[k] /= l2;
-    o[0] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)dot(n, a));
-    o[1] = make_float4((float)n1[0], (float)n1[1], (float)n1[2], (float)-dot(n1, a));
-    o[2] = make_float4((float)n2[0], (float)n2[1], (float)n2[2], (float)-dot(n2, a));
-  }
-  return out;
-}
-
 // The arrays are present and their counts within the encodings' limits.
 ct_status validate_pointers(const ct_packed_scene_view& v) {
   CT_CHECK_ARG(v.node_count == 0 || v.nodes != nullptr, "nodes is NULL");
@@ -388,6 +343,57 @@ __global__ void k_compact_prims(const float4* __restrict__ prims, uint32_t n, fl
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += stride) {
     const size_t p = i / 3;
     tris[i] = __ldg(prims + p * 4 + (i - p * 3));
+  }
+}
+
+// Plane records of the integrator's float32 triangle test, 48 bytes per
+// primitive (Havel and Herout, "Yet Faster Ray-Triangle Intersection (Using
+// SSE4)", IEEE TVCG 16(3), 2010). For a triangle (a, b, c) with
+// n = (b-a) x (c-a): [n, n.a | n1, -n1.a | n2, -n2.a] with
+// n1 = ((c-a) x n)/|n|^2 and n2 = (n x (b-a))/|n|^2, computed in float64
+// with every operation rounded separately (no fused multiply-adds) and
+// rounded once to float32; a sphere stores its centre and radius and a NaN
+// marker; a degenerate triangle stores zeros. Built on the device from the
+// uploaded primitives, one thread per primitive, so the host neither
+// computes nor uploads them.
+__global__ void k_plane_records(const float4* __restrict__ prims, uint32_t n, float4* __restrict__ planes) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += stride) {
+    const float4 q0 = prims[p * 4], q1 = prims[p * 4 + 1], q2 = prims[p * 4 + 2];
+    float4* o = planes + p * 3;
+    if (q0.w == (float)CT_PRIM_SPHERE) {
+      o[0] = make_float4(q0.x, q0.y, q0.z, q1.x);
+      o[1] = make_float4(__int_as_float(0x7fc00000), 0.0f, 0.0f, 0.0f);
+      o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      continue;
+    }
+    auto sub = [](double x, double y) { return __dsub_rn(x, y); };
+    auto mul = [](double x, double y) { return __dmul_rn(x, y); };
+    auto add = [](double x, double y) { return __dadd_rn(x, y); };
+    const double a[3] = {q0.x, q0.y, q0.z};
+    const double e1[3] = {sub(q1.x, a[0]), sub(q1.y, a[1]), sub(q1.z, a[2])};
+    const double e2[3] = {sub(q2.x, a[0]), sub(q2.y, a[1]), sub(q2.z, a[2])};
+    auto cross = [&](const double* x, const double* y, double* z) {
+      z[0] = sub(mul(x[1], y[2]), mul(x[2], y[1]));
+      z[1] = sub(mul(x[2], y[0]), mul(x[0], y[2]));
+      z[2] = sub(mul(x[0], y[1]), mul(x[1], y[0]));
+    };
+    auto dot = [&](const double* x, const double* y) {
+      return add(add(mul(x[0], y[0]), mul(x[1], y[1])), mul(x[2], y[2]));
+    };
+    double nn[3], n1[3], n2[3];
+    cross(e1, e2, nn);
+    const double l2 = dot(nn, nn);
+    if (!(l2 > 0.0) || !isfinite(l2)) {
+      o[0] = o[1] = o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      continue;
+    }
+    cross(e2, nn, n1);
+    cross(nn, e1, n2);
+    for (int k = 0; k < 3; k++) n1[k] = __ddiv_rn(n1[k], l2), n2[k] = __ddiv_rn(n2[k], l2);
+    o[0] = make_float4((float)nn[0], (float)nn[1], (float)nn[2], (float)dot(nn, a));
+    o[1] = make_float4((float)n1[0], (float)n1[1], (float)n1[2], (float)-dot(n1, a));
+    o[2] = make_float4((float)n2[0], (float)n2[1], (float)n2[2], (float)-dot(n2, a));
   }
 }
 
@@ -460,45 +466,33 @@ void destroy(ct_scene* s) {
   delete s;
 }
 
-// Scenes of at least this many primitives run their independent host passes
-// on separate threads (caustic scene, 327,746 primitives: the create call's
-// host work drops to the tree check and record build; below this size the
-// threads cost more than they save).
+// Scenes of at least this many primitives run the value checks on a separate
+// thread, beside the tree check and record build (caustic scene, 327,746
+// primitives; below this size the thread costs more than it saves).
 constexpr uint32_t kThreadedPrims = 50000;
 
 ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
   ct_status st = validate_pointers(v);
   if (st != CT_OK) return st;
-  // The value checks and the plane records read only the primitive,
-  // material and light arrays, so they run beside the tree check, the
-  // record build and the half records (which follow the check).
+  // The value checks read only the primitive, material and light arrays, so
+  // they run beside the tree check, the record build and the half records
+  // (which follow the check). The plane records and the compact triangles
+  // are built on the device from the uploaded primitives.
   const bool threaded = v.prim_count >= kThreadedPrims;
   ct_status values = CT_OK;
-  std::vector<float4> planes;
-  bool planes_oom = false;
-  auto plane_pass = [&] {
-    try {
-      planes = plane_records(v);
-    } catch (const std::bad_alloc&) {
-      planes_oom = true;
-    }
-  };
-  std::thread t_values, t_planes;
+  std::thread t_values;
   if (threaded) {
     try {
       t_values = std::thread([&] { values = validate_view(v); });
-      t_planes = std::thread(plane_pass);
-    } catch (const std::exception&) {  // no threads: the passes run on this thread below
+    } catch (const std::exception&) {  // no thread: the checks run on this thread below
     }
   }
-  struct Joiner {  // every return below joins the worker threads first
+  struct Joiner {  // every return below joins the worker thread first
     std::thread& a;
-    std::thread& b;
     ~Joiner() {
       if (a.joinable()) a.join();
-      if (b.joinable()) b.join();
     }
-  } joiner{t_values, t_planes};
+  } joiner{t_values};
   if (!t_values.joinable()) {
     st = validate_view(v);
     if (st != CT_OK) return st;
@@ -523,12 +517,6 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
     // the error message belongs to the calling thread: run the check again here
     if (values != CT_OK) return validate_view(v);
   }
-  if (t_planes.joinable()) {
-    t_planes.join();
-  } else {
-    plane_pass();
-  }
-  if (planes_oom) return fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");
 
   ct_scene* s = new (std::nothrow) ct_scene();
   if (!s) return fail(CT_ERR_OUT_OF_MEMORY, "ct_scene_create: host allocation failed");
@@ -570,7 +558,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
                        arena_slot(std::max<size_t>(v.mat_count * 4, 4) * sizeof(float4)) +
                        arena_slot(std::max<size_t>(v.light_count, 1) * sizeof(int32_t)) +
                        arena_slot(std::max<size_t>(v.prim_count, 1) * sizeof(uint32_t)) +
-                       arena_slot(std::max<size_t>(planes.size(), 3) * sizeof(float4)) +
+                       arena_slot(std::max<size_t>((size_t)v.prim_count * 3, 3) * sizeof(float4)) +
                        arena_slot(std::max<size_t>((size_t)v.prim_count * 3, 3) * sizeof(float4)) +
                        arena_slot(kCounterWords * sizeof(uint32_t));
   if ((st = path_alloc(s->device, arena, s->stream, &s->arena)) != CT_OK) return bail(st);
@@ -582,7 +570,7 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
       (st = upload(s, s->mats, cursor, reinterpret_cast<const float4*>(v.mats), (size_t)v.mat_count * 4, 4)) != CT_OK ||
       (st = upload(s, s->lights, cursor, v.lights, v.light_count, 1)) != CT_OK ||
       (st = upload(s, s->prim_object, cursor, v.prim_object, v.prim_count, 1)) != CT_OK ||
-      (st = upload(s, s->planes, cursor, planes.data(), planes.size(), 3)) != CT_OK ||
+      (st = carve(s, s->planes, cursor, std::max<size_t>((size_t)v.prim_count * 3, 3) * sizeof(float4))) != CT_OK ||
       (st = carve(s, s->tris, cursor, std::max<size_t>((size_t)v.prim_count * 3, 3) * sizeof(float4))) != CT_OK ||
       (st = upload(s, s->counters, cursor, (const uint32_t*)nullptr, 0, kCounterWords)) != CT_OK)
     return bail(st);
@@ -590,10 +578,14 @@ ct_status create(const ct_packed_scene_view& v, ct_scene** out) {
     const size_t total = (size_t)v.prim_count * 3;
     const unsigned blocks = (unsigned)std::min<size_t>((total + 255) / 256, 4096);
     k_compact_prims<<<blocks, 256, 0, s->stream>>>(s->prims.as<float4>(), v.prim_count, s->tris.as<float4>());
+    const unsigned plane_blocks = (unsigned)std::min<size_t>(((size_t)v.prim_count + 127) / 128, 4096);
+    k_plane_records<<<plane_blocks, 128, 0, s->stream>>>(s->prims.as<float4>(), v.prim_count,
+                                                         s->planes.as<float4>());
     cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "k_compact_prims: %s", cudaGetErrorString(err)));
+    if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "scene records: %s", cudaGetErrorString(err)));
   } else {
     cudaError_t err = cudaMemsetAsync(s->tris.ptr, 0, s->tris.bytes, s->stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(s->planes.ptr, 0, s->planes.bytes, s->stream);
     if (err != cudaSuccess) return bail(fail(CT_ERR_CUDA, "scene upload: %s", cudaGetErrorString(err)));
   }
   if (v.mat_count == 0 && v.mats != nullptr) {
