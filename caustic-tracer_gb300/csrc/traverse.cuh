@@ -596,8 +596,13 @@ struct WalkStack {
 // ray's three 16-byte groups) the exact walk runs at 912 against 896; with
 // the counters read and written once per step (WalkCtl) at 1,049 against
 // 968 (and the integrator's walk, caustic scene, at 1,969 against 1,915).
+// The exact walk's lane also keeps its query number and fallback count in
+// the frame: they change once per query (or never), and the registers they
+// free spare the step's spill slots (spill stores 72 -> 44 bytes; 1M soup
+// 1,093 -> 1,109 Mrays/s).
 struct WalkFrame {
   Walk w;
+  uint32_t idx, fallbacks;
   WalkStack st;
 };
 
@@ -744,7 +749,11 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
   Walk& w = EXACT ? frame.w : apart;
   WalkStack& st = EXACT ? frame.st : apart_stack;
   w.c.ref = kWalkDone;
-  uint32_t idx = kNoQuery;  // query held by this lane
+  uint32_t idx_reg = kNoQuery;
+  uint32_t& idx = EXACT ? frame.idx : idx_reg;  // query held by this lane
+  idx = kNoQuery;
+  frame.fallbacks = 0;
+  uint32_t& fb = EXACT ? frame.fallbacks : fallbacks;
   bool drained = false;
   for (;;) {
     const bool idle = w.c.ref == kWalkDone;
@@ -767,7 +776,10 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
         }
       }
     }
-    if (__all_sync(0xffffffffu, idx == kNoQuery) && drained) break;
+    if (__all_sync(0xffffffffu, idx == kNoQuery) && drained) {
+      if (EXACT) fallbacks += frame.fallbacks;
+      break;
+    }
     // One copy of the step in the loop body (not unrolled): the integrator's
     // walk runs 1 % faster on the caustic scene, the exact walk unchanged
     // with half the spill slots.
@@ -779,7 +791,7 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
         const uint32_t inner = __ballot_sync(0xffffffffu, w.c.ref >= 0);
         go = go && (w.c.ref == kWalkLeaf) == (__popc(leaf) >= __popc(inner));
       }
-      if (go) walk_step<EXACT, UV, ANYQ>(s, w, st, fallbacks);
+      if (go) walk_step<EXACT, UV, ANYQ>(s, w, st, fb);
     }
   }
 }
