@@ -578,9 +578,15 @@ struct alignas(16) Walk {
 };
 
 // The walk stack: (child reference, entry distance bits), one 8-byte access
-// per push or pop, in local memory.
+// per push or pop, in local memory. Beside it the lane's query number and
+// fallback count: they change once per query (or never), and keeping them
+// in local memory instead of registers spares the step's spill slots (exact
+// walk: spill stores 72 -> 44 bytes, 1M soup 1,093 -> 1,109 Mrays/s;
+// integrator: caustic scene 2,176 -> 2,194 Msamples/s, batched soups
+// 1,450 -> 1,457).
 struct WalkStack {
   int2 e[kStackSize];
+  uint32_t idx, fallbacks;
 };
 
 // A walk's state and stack as one object. An array indexed at run time keeps
@@ -596,13 +602,8 @@ struct WalkStack {
 // ray's three 16-byte groups) the exact walk runs at 912 against 896; with
 // the counters read and written once per step (WalkCtl) at 1,049 against
 // 968 (and the integrator's walk, caustic scene, at 1,969 against 1,915).
-// The exact walk's lane also keeps its query number and fallback count in
-// the frame: they change once per query (or never), and the registers they
-// free spare the step's spill slots (spill stores 72 -> 44 bytes; 1M soup
-// 1,093 -> 1,109 Mrays/s).
 struct WalkFrame {
   Walk w;
-  uint32_t idx, fallbacks;
   WalkStack st;
 };
 
@@ -749,11 +750,10 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
   Walk& w = EXACT ? frame.w : apart;
   WalkStack& st = EXACT ? frame.st : apart_stack;
   w.c.ref = kWalkDone;
-  uint32_t idx_reg = kNoQuery;
-  uint32_t& idx = EXACT ? frame.idx : idx_reg;  // query held by this lane
+  uint32_t& idx = st.idx;  // query held by this lane
   idx = kNoQuery;
-  frame.fallbacks = 0;
-  uint32_t& fb = EXACT ? frame.fallbacks : fallbacks;
+  st.fallbacks = 0;
+  uint32_t& fb = st.fallbacks;
   bool drained = false;
   for (;;) {
     const bool idle = w.c.ref == kWalkDone;
@@ -777,7 +777,7 @@ __device__ __forceinline__ void walk_persistent(Scene& s, uint32_t* counter, uin
       }
     }
     if (__all_sync(0xffffffffu, idx == kNoQuery) && drained) {
-      if (EXACT) fallbacks += frame.fallbacks;
+      fallbacks += st.fallbacks;
       break;
     }
     // One copy of the step in the loop body (not unrolled): the integrator's
