@@ -1162,6 +1162,7 @@ def run_served(args, rank, world, emit=True):
     res_s, _, _, srv_s = served(rate)
     res_f, _, _, _ = served(rate, "fifo")
     res_r, _, _, _ = served(rate, "srpt")
+    res_a, _, _, _ = served(rate, "srpt_age")
     res_p, _ = plain(rate)
     if args.trace == "preview":
         mix = "preview mix: sides 128-256 squared, 1-8 spp"
@@ -1194,7 +1195,8 @@ def run_served(args, rank, world, emit=True):
         "speedup_vs_per_frame": value / frame_rate,
         "latency": {"arrivals": f"Poisson, {rate:.1f} requests/s (80% of the plain path's capacity)",
                     "served": latency_stats(res_s), "served_fifo": latency_stats(res_f),
-                    "served_srpt": latency_stats(res_r), "plain": latency_stats(res_p),
+                    "served_srpt": latency_stats(res_r), "served_srpt_age": latency_stats(res_a),
+                    "plain": latency_stats(res_p),
                     "served_steps": srv_s.steps},
         "clocks": clocks.summary(),
         "e2e": {"value": samples * args.steps * world / t_wall / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0,

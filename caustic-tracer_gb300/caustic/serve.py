@@ -93,14 +93,16 @@ class Executor(Protocol):
 
 
 class RenderServer:
-    POLICIES = ("round_robin", "fifo", "srpt")
+    POLICIES = ("round_robin", "fifo", "srpt", "srpt_age")
 
     def __init__(self, executor: Executor, budget_bytes: int = 120 << 30, step_paths: int = 16 << 20,
                  min_chunk_paths: int = 16 << 20, max_passes_per_step: Optional[int] = None,
-                 clock: Callable[[], float] = time.perf_counter, policy: str = "round_robin"):
+                 clock: Callable[[], float] = time.perf_counter, policy: str = "round_robin",
+                 age_limit: float = 0.10):
         if policy not in self.POLICIES:
             raise ValueError(f"policy {policy!r} is not one of {self.POLICIES}")
         self.policy = policy
+        self.age_limit = float(age_limit)
         self.ex = executor
         self.budget = int(budget_bytes)
         self.step_paths = int(step_paths)
@@ -189,7 +191,10 @@ class RenderServer:
         the oldest (a large request runs as fast as alone, later ones only fill
         what is left of each wave), or srpt: the fewest samples left first
         (small requests go ahead of large ones, and a large request is not
-        spread over the steps of many others; ties by admission order). Each request gets an equal share of the
+        spread over the steps of many others; ties by admission order), or
+        srpt_age: srpt among the requests that arrived less than age_limit
+        seconds ago, every older one first in admission order (a large
+        request waits at most about age_limit behind smaller ones). Each request gets an equal share of the
         step, but at least min_chunk_paths (a request's chunk keeps its scene
         hot in L2 for a while) and at least one pass, at most what it still
         needs and what still fits; requests that do not fit wait for the next
@@ -203,6 +208,10 @@ class RenderServer:
             pending = pending[k:] + pending[:k]
         elif self.policy == "srpt":
             pending.sort(key=lambda a: ((a.req.spp - a.issued) * a.req.pixels, a.seq))
+        elif self.policy == "srpt_age":
+            now = self.clock()
+            pending.sort(key=lambda a: (0, a.seq, 0) if now - a.req.arrival > self.age_limit
+                         else (1, (a.req.spp - a.issued) * a.req.pixels, a.seq))
         cls = self.ex.walk_class(pending[0].req.scene)
         share = max(self.step_paths / len(pending), min(self.min_chunk, self.step_paths))
         room = self.step_paths

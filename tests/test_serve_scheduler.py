@@ -246,3 +246,21 @@ def test_srpt_policy_runs_the_request_with_least_work_left_first():
         assert [f for f, _ in r.image] == sorted(f for f, _ in r.image)
         assert sum(p for _, p in r.image) == r.request.spp
 
+
+def test_srpt_age_policy_serves_overdue_requests_first():
+    ex = FakeExecutor({"a": 0})
+    step_paths = 64 * 64 * 4
+    clock = Clock()
+    srv = RenderServer(ex, budget_bytes=1 << 40, step_paths=step_paths, clock=clock, policy="srpt_age",
+                       age_limit=0.5)
+    old = _req(0, 64, 12, arrival=-1.0)   # large and already overdue
+    srv.submit(old)
+    srv.submit(_req(1, 16, 4, arrival=clock.t + 1.0))  # small and fresh
+    srv.step()
+    first = dict((r, p) for r, _, p in ex.steps[0])
+    assert first[0] == 4  # the overdue request takes the whole step despite its size
+    srv.drain()
+    assert {r.request.rid for r in srv.results} == {0, 1}
+    for r in srv.results:
+        assert sum(p for _, p in r.image) == r.request.spp
+
